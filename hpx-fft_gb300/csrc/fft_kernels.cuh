@@ -1,0 +1,550 @@
+// Device side of the 2D real-to-complex transform.
+//
+// The reference (core/src/shared/loop.cpp:56-113) runs four phases over host
+// memory: row r2c (FFTW), transpose, column c2c (FFTW), transpose back.  Here
+// the two transposes disappear: the column kernel works on strips of W
+// adjacent ky columns directly in the [kx][ky] layout, so the whole 2D
+// transform is two HBM passes (row pass: read S, write S; column pass: read S,
+// write S) over the caller's padded in-place buffer.
+//
+// One 1D transform of length N is held in shared memory.  When it does not
+// fit one CTA it is split over a thread-block cluster of C CTAs: CTA c owns
+// the inputs n = c + C*m, runs a length-N/C Stockham FFT on them, multiplies
+// by W_N^(c*k2), and the length-C DFTs across the cluster read the peers'
+// shared memory (DSMEM).  The result index is k = k2 + (N/C)*k1.
+#pragma once
+#include <cooperative_groups.h>
+
+#include "cplx.cuh"
+
+namespace hpxfft_gpu {
+namespace cg = cooperative_groups;
+
+constexpr int kMaxPasses = 24;
+// Radix sequence of one local Stockham transform (radices 2,3,4,5,8,16).
+struct PassPlan {
+    int n;
+    int radix[kMaxPasses];
+};
+
+// Compute-type traits: T = arithmetic type, S = storage (HBM) real type.
+struct ArithF32 {
+    using T = float;
+    using S = float;
+    static constexpr bool kScaled = false;
+    static constexpr int kMaxThreads = 1024;
+};
+struct ArithF64 {
+    using T = double;
+    using S = double;
+    static constexpr bool kScaled = false;
+    static constexpr int kMaxThreads = 512;
+};
+struct ArithFF {
+    using T = ff;
+    using S = double;
+    static constexpr bool kScaled = true;  // per-transform power-of-two scale
+    static constexpr int kMaxThreads = 512;
+};
+
+// Elements held per thread in every pass (16 complex values).
+constexpr int kElemsPerThread = 16;
+
+// ----------------------------------------------------------------- storage
+template <class A>
+__device__ __forceinline__ cpx<typename A::T> load_c(const typename A::S *p, int E)
+{
+    using S = typename A::S;
+    if constexpr (A::kScaled) {
+        const double2 v = *reinterpret_cast<const double2 *>(p);
+        return cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
+    } else if constexpr (sizeof(S) == 8) {
+        const double2 v = *reinterpret_cast<const double2 *>(p);
+        return cpx<double>{v.x, v.y};
+    } else {
+        const float2 v = *reinterpret_cast<const float2 *>(p);
+        return cpx<float>{v.x, v.y};
+    }
+}
+
+template <class A>
+__device__ __forceinline__ void store_c(typename A::S *p, cpx<typename A::T> v, int E)
+{
+    if constexpr (A::kScaled) {
+        double2 o;
+        o.x = ff_to_double(renorm(v.re), E);
+        o.y = ff_to_double(renorm(v.im), E);
+        *reinterpret_cast<double2 *>(p) = o;
+    } else if constexpr (sizeof(typename A::S) == 8) {
+        *reinterpret_cast<double2 *>(p) = make_double2(v.re, v.im);
+    } else {
+        *reinterpret_cast<float2 *>(p) = make_float2(v.re, v.im);
+    }
+}
+
+__device__ __forceinline__ int scale_exp(int emax) { return (emax == 0 || emax == 0x7ff) ? 0 : emax - 1023; }
+
+// twiddle W_Ltab^e (table holds the forward sign); DIR > 0 conjugates
+template <int DIR, class T>
+__device__ __forceinline__ cpx<T> twid(const cpx<T> *__restrict__ tw, int e)
+{
+    cpx<T> w = tw[e];
+    if constexpr (DIR > 0) w.im = -w.im;
+    return w;
+}
+
+// ----------------------------------------------------------- Stockham pass
+// One radix-R pass of a self-sorting (Stockham, decimation in time) FFT on W
+// interleaved transforms of length L held in shared memory as s[n*W + w].
+// Ls = length of the sub-transforms already combined.  Every thread keeps its
+// tasks in registers across the barrier, so the pass works in place.
+template <class T, int R, int DIR>
+__device__ __forceinline__ void fft_pass(cpx<T> *s, int L, int log2W, int Ls, const cpx<T> *__restrict__ tw,
+                                         int Ltab)
+{
+    constexpr int TPT = (kElemsPerThread + R - 1) / R;
+    const int LR = L / R;
+    const int ntask = LR << log2W;
+    const int wmask = (1 << log2W) - 1;
+    const int step = Ltab / (Ls * R);
+    cpx<T> v[TPT][R];
+#pragma unroll
+    for (int t = 0; t < TPT; ++t) {
+        const int task = threadIdx.x + t * blockDim.x;
+        if (task < ntask) {
+            const int w = task & wmask, jj = task >> log2W;
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[t][r] = s[((jj + r * LR) << log2W) + w];
+            if (Ls > 1) {
+                const int k = jj % Ls;
+#pragma unroll
+                for (int r = 1; r < R; ++r) v[t][r] = cmul(v[t][r], twid<DIR>(tw, r * k * step));
+            }
+            DFT<R, DIR, T>::run(v[t]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < TPT; ++t) {
+        const int task = threadIdx.x + t * blockDim.x;
+        if (task < ntask) {
+            const int w = task & wmask, jj = task >> log2W;
+            const int k = jj % Ls;
+            const int base = (jj - k) * R + k;  // (jj / Ls) * Ls * R + k
+#pragma unroll
+            for (int r = 0; r < R; ++r) s[((base + r * Ls) << log2W) + w] = cnorm(v[t][r]);
+        }
+    }
+    __syncthreads();
+}
+
+template <class T, int DIR>
+__device__ void local_fft(cpx<T> *s, int L, int log2W, const PassPlan &pp, const cpx<T> *__restrict__ tw, int Ltab)
+{
+    int Ls = 1;
+    for (int p = 0; p < pp.n; ++p) {
+        const int R = pp.radix[p];
+        switch (R) {
+        case 16: fft_pass<T, 16, DIR>(s, L, log2W, Ls, tw, Ltab); break;
+        case 8: fft_pass<T, 8, DIR>(s, L, log2W, Ls, tw, Ltab); break;
+        case 4: fft_pass<T, 4, DIR>(s, L, log2W, Ls, tw, Ltab); break;
+        case 2: fft_pass<T, 2, DIR>(s, L, log2W, Ls, tw, Ltab); break;
+        case 3: fft_pass<T, 3, DIR>(s, L, log2W, Ls, tw, Ltab); break;
+        case 5: fft_pass<T, 5, DIR>(s, L, log2W, Ls, tw, Ltab); break;
+        default: break;
+        }
+        Ls *= R;
+    }
+}
+
+// Largest input exponent per interleaved transform w, reduced over the CTA and
+// (C > 1) over the cluster.  Every thread's elements share w = tid & (W-1).
+template <int C>
+__device__ __forceinline__ void reduce_exponents(int emax, int log2W, int *sE, int *sEc)
+{
+    const int W = 1 << log2W;
+    for (int off = 16; off >= W; off >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, off));
+    if ((threadIdx.x & 31) < W) atomicMax(&sE[threadIdx.x & (W - 1)], emax);
+    if constexpr (C > 1) {
+        cg::cluster_group cl = cg::this_cluster();
+        cl.sync();
+        if (threadIdx.x < (unsigned)W) {
+            int e = 0;
+            for (int r = 0; r < C; ++r) e = max(e, *cl.map_shared_rank(&sE[threadIdx.x], r));
+            sEc[threadIdx.x] = e;
+        }
+    } else {
+        __syncthreads();
+        if (threadIdx.x < (unsigned)W) sEc[threadIdx.x] = sE[threadIdx.x];
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------- arguments
+struct RowArgs {
+    const void *in;           // real rows (r2c) or complex rows (c2r)
+    void *out;                // complex rows (r2c) or real rows (c2r)
+    long long in_stride;      // reals per input row
+    long long out_stride;     // reals per output row
+    long long in_bstride;     // reals between batch items
+    long long out_bstride;
+    int nrows;
+    int M;                    // ny / 2
+    int log2W;                // rows per CTA = 1 << log2W (only with C == 1)
+    int adjoint;              // c2r: half weights on the interior bins
+    PassPlan pp;              // local transform of length M / C
+    const void *tw;           // W_{2M}^e, e in [0, 2M)
+    int Ltab;                 // 2M
+};
+
+struct ColArgs {
+    void *data;               // complex [nx][ncols] rows, in place
+    long long row_stride;     // reals per row (2 * ncols for the padded layout)
+    long long bstride;
+    int nx;
+    int ncols;
+    int log2W;                // columns per strip
+    PassPlan pp;              // local transform of length nx / C
+    const void *tw;           // W_nx^e, e in [0, nx)
+    int Ltab;                 // nx
+};
+
+// ------------------------------------------------------------ row r2c kernel
+// Packed-real row transform: z[m] = x[2m] + i x[2m+1], Z = DFT_M(z), then
+//   X[k] = E - i W_2M^k O,  X[M-k] = conj(E + i W_2M^k O),
+//   E = (Z[k] + conj Z[M-k]) / 2,  O = (Z[k] - conj Z[M-k]) / 2.
+// Replaces the FFTW row pass core/src/shared/loop.cpp:61-69 (fft_1d_r2c_inplace,
+// loop.cpp:6-9); output row kx holds X[kx][0..M] in place of the padded input.
+template <class A, int C>
+__global__ void __launch_bounds__(A::kMaxThreads, 1) row_r2c_kernel(RowArgs a)
+{
+    using T = typename A::T;
+    using S = typename A::S;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cpx<T> *s = reinterpret_cast<cpx<T> *>(smem_raw);
+    __shared__ int sE[16], sEc[16];
+    const int log2W = a.log2W, W = 1 << log2W, wmask = W - 1;
+    const int M = a.M, L = M / C;
+    unsigned crank = 0;
+    if constexpr (C > 1) crank = cg::this_cluster().block_rank();
+    const int row0 = (blockIdx.x / C) * W;
+    const S *in = reinterpret_cast<const S *>(a.in) + (long long)blockIdx.y * a.in_bstride;
+    S *out = reinterpret_cast<S *>(a.out) + (long long)blockIdx.y * a.out_bstride;
+    const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
+    const int tid = threadIdx.x, nth = blockDim.x, nel = L << log2W;
+
+    if constexpr (A::kScaled) {
+        if (tid < 16) sE[tid] = 0;
+        __syncthreads();
+        int emax = 0;
+        for (int t = tid; t < nel; t += nth) {
+            const int w = t & wmask, m = t >> log2W, row = row0 + w;
+            double2 v = make_double2(0.0, 0.0);
+            if (row < a.nrows) {
+                const long long n = crank + (long long)C * m;
+                v = *reinterpret_cast<const double2 *>(in + row * a.in_stride + 2 * n);
+            }
+            reinterpret_cast<double2 *>(s)[t] = v;
+            emax = max(emax, max(dbl_biased_exp(v.x), dbl_biased_exp(v.y)));
+        }
+        reduce_exponents<C>(emax, log2W, sE, sEc);
+        for (int t = tid; t < nel; t += nth) {
+            const double2 v = reinterpret_cast<double2 *>(s)[t];
+            const int E = scale_exp(sEc[t & wmask]);
+            s[t] = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
+        }
+    } else {
+        for (int t = tid; t < nel; t += nth) {
+            const int w = t & wmask, m = t >> log2W, row = row0 + w;
+            cpx<T> v = czero<T>();
+            if (row < a.nrows) v = load_c<A>(in + row * a.in_stride + 2 * (crank + (long long)C * m), 0);
+            s[t] = v;
+        }
+    }
+    __syncthreads();
+
+    local_fft<T, -1>(s, L, log2W, a.pp, tw, a.Ltab);
+
+    if constexpr (C == 1) {
+        const int ntask = (M / 2 + 1) << log2W;
+        for (int t = tid; t < ntask; t += nth) {
+            const int w = t & wmask, k = t >> log2W, row = row0 + w;
+            if (row >= a.nrows) continue;
+            const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
+            const cpx<T> za = s[(k << log2W) + w];
+            const cpx<T> zb = cconj(s[(((M - k) % M) << log2W) + w]);
+            const cpx<T> e = chalf(za + zb), o = chalf(za - zb);
+            const cpx<T> tk = cmul(tw[k], o);
+            S *orow = out + row * a.out_stride;
+            store_c<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk), E);
+            if (M - k != k) store_c<A>(orow + 2 * (long long)(M - k), cconj(e + mul_i<+1>(tk)), E);
+        }
+    } else {
+        cg::cluster_group cl = cg::this_cluster();
+        const int E = A::kScaled ? scale_exp(sEc[0]) : 0;
+        // W_M^(c k2) = W_2M^(2 c k2)
+        if (crank > 0)
+            for (int t = tid; t < L; t += nth) s[t] = cnorm(cmul(s[t], tw[2 * (int)crank * t]));
+        cl.sync();
+        const int Lc = L / C, k20 = crank * Lc;
+        constexpr int TPT = kElemsPerThread / C;
+        cpx<T> v[TPT][C];
+#pragma unroll
+        for (int u = 0; u < TPT; ++u) {
+            const int t = tid + u * nth;
+            if (t < Lc) {
+#pragma unroll
+                for (int r = 0; r < C; ++r) v[u][r] = *cl.map_shared_rank(&s[k20 + t], r);
+                DFT<C, -1, T>::run(v[u]);
+            }
+        }
+        cl.sync();
+#pragma unroll
+        for (int u = 0; u < TPT; ++u) {
+            const int t = tid + u * nth;
+            if (t < Lc)
+#pragma unroll
+                for (int k1 = 0; k1 < C; ++k1) s[t + Lc * k1] = cnorm(v[u][k1]);
+        }
+        cl.sync();
+        // my Z[k], k = k20 + (li % Lc) + L * (li / Lc), sit at local index li
+        for (int li = tid; li < L; li += nth) {
+            const int k1 = li / Lc, k2 = k20 + li % Lc;
+            const int k = k2 + L * k1;
+            const int kp = (M - k) % M;
+            const int k2p = kp % L, cp = k2p / Lc;
+            const int lip = (k2p - cp * Lc) + Lc * (kp / L);
+            const cpx<T> za = s[li];
+            const cpx<T> zb = cconj(*cl.map_shared_rank(&s[lip], cp));
+            const cpx<T> e = chalf(za + zb), o = chalf(za - zb);
+            const cpx<T> tk = cmul(tw[k], o);
+            S *orow = out + row0 * a.out_stride;
+            if (row0 < a.nrows) {
+                store_c<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk), E);
+                if (k == 0) store_c<A>(orow + 2 * (long long)M, cconj(e + mul_i<+1>(tk)), E);
+            }
+        }
+        cl.sync();
+    }
+}
+
+// ------------------------------------------------------------ row c2r kernel
+// Unnormalised c2r of a Hermitian half spectrum X[0..M] (imaginary parts of
+// X[0], X[M] ignored):  Z[k] = (X[k] + conj X[M-k]) + i W_2M^-k (X[k] - conj X[M-k]),
+// z = IDFT_M(Z) unnormalised, x[2m] = Re z[m], x[2m+1] = Im z[m].  With
+// `adjoint` the interior bins are halved first, which turns the c2r into the
+// adjoint of the r2c.  No reference counterpart (the FFTW backward direction
+// is declared in core/include/hpxfft/util/adapter_fftw.hpp:11 but unused).
+template <class A, int C>
+__global__ void __launch_bounds__(A::kMaxThreads, 1) row_c2r_kernel(RowArgs a)
+{
+    using T = typename A::T;
+    using S = typename A::S;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cpx<T> *s = reinterpret_cast<cpx<T> *>(smem_raw);
+    __shared__ int sE[16], sEc[16];
+    const int log2W = a.log2W, W = 1 << log2W, wmask = W - 1;
+    const int M = a.M, L = M / C;
+    unsigned crank = 0;
+    if constexpr (C > 1) crank = cg::this_cluster().block_rank();
+    const int row0 = (blockIdx.x / C) * W;
+    const S *in = reinterpret_cast<const S *>(a.in) + (long long)blockIdx.y * a.in_bstride;
+    S *out = reinterpret_cast<S *>(a.out) + (long long)blockIdx.y * a.out_bstride;
+    const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
+    const int tid = threadIdx.x, nth = blockDim.x, nel = L << log2W;
+
+    int emax = 0;
+    if constexpr (A::kScaled) {
+        if (tid < 16) sE[tid] = 0;
+        __syncthreads();
+        for (int t = tid; t < nel; t += nth) {
+            const int w = t & wmask, m = t >> log2W, row = row0 + w;
+            const int k = crank + C * m;
+            double2 v = make_double2(0.0, 0.0), u = make_double2(0.0, 0.0);
+            if (row < a.nrows) {
+                v = *reinterpret_cast<const double2 *>(in + row * a.in_stride + 2 * (long long)k);
+                u = *reinterpret_cast<const double2 *>(in + row * a.in_stride + 2 * (long long)(M - k));
+            }
+            reinterpret_cast<double2 *>(s)[t] = v;
+            emax = max(emax, max(max(dbl_biased_exp(v.x), dbl_biased_exp(v.y)),
+                                 max(dbl_biased_exp(u.x), dbl_biased_exp(u.y))));
+        }
+        reduce_exponents<C>(emax, log2W, sE, sEc);
+    }
+    for (int t = tid; t < nel; t += nth) {
+        const int w = t & wmask, m = t >> log2W, row = row0 + w;
+        const int k = crank + C * m;
+        const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
+        cpx<T> xa = czero<T>(), xb = czero<T>();
+        if (row < a.nrows) {
+            if constexpr (A::kScaled) {
+                const double2 v = reinterpret_cast<double2 *>(s)[t];
+                xa = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
+            } else {
+                xa = load_c<A>(in + row * a.in_stride + 2 * (long long)k, 0);
+            }
+            xb = load_c<A>(in + row * a.in_stride + 2 * (long long)(M - k), E);
+        }
+        if (k == 0) {
+            xa.im = real_ops<T>::zero();
+            xb.im = real_ops<T>::zero();
+        } else if (a.adjoint) {
+            xa = chalf(xa);
+            xb = chalf(xb);
+        }
+        const cpx<T> xbc = cconj(xb);
+        const cpx<T> sum = xa + xbc, dif = xa - xbc;
+        s[t] = cnorm(sum + mul_i<+1>(cmul(twid<+1>(tw, k), dif)));
+    }
+    __syncthreads();
+
+    local_fft<T, +1>(s, L, log2W, a.pp, tw, a.Ltab);
+
+    if constexpr (C == 1) {
+        for (int t = tid; t < nel; t += nth) {
+            const int w = t & wmask, m = t >> log2W, row = row0 + w;
+            if (row >= a.nrows) continue;
+            const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
+            store_c<A>(out + row * a.out_stride + 2 * (long long)m, s[t], E);
+            if (m == 0) {
+                out[row * a.out_stride + 2 * (long long)M] = (S)0;
+                out[row * a.out_stride + 2 * (long long)M + 1] = (S)0;
+            }
+        }
+    } else {
+        cg::cluster_group cl = cg::this_cluster();
+        const int E = A::kScaled ? scale_exp(sEc[0]) : 0;
+        if (crank > 0)
+            for (int t = tid; t < L; t += nth) s[t] = cnorm(cmul(s[t], twid<+1>(tw, 2 * (int)crank * t)));
+        cl.sync();
+        const int Lc = L / C, k20 = crank * Lc;
+        for (int t = tid; t < Lc; t += nth) {
+            cpx<T> v[C];
+#pragma unroll
+            for (int r = 0; r < C; ++r) v[r] = *cl.map_shared_rank(&s[k20 + t], r);
+            DFT<C, +1, T>::run(v);
+            if (row0 < a.nrows)
+#pragma unroll
+                for (int k1 = 0; k1 < C; ++k1)
+                    store_c<A>(out + row0 * a.out_stride + 2 * (long long)(k20 + t + L * k1), v[k1], E);
+        }
+        if (crank == 0 && tid == 0 && row0 < a.nrows) {
+            out[row0 * a.out_stride + 2 * (long long)M] = (S)0;
+            out[row0 * a.out_stride + 2 * (long long)M + 1] = (S)0;
+        }
+        cl.sync();
+    }
+}
+
+// ------------------------------------------------------------- column kernel
+// In-place length-nx c2c on strips of W adjacent columns of the [kx][ky]
+// array.  Replaces transpose -> FFTW c2c -> transpose back
+// (core/src/shared/loop.cpp:72-102, fft_1d_c2c_inplace loop.cpp:11-15).
+template <class A, int C, int DIR>
+__global__ void __launch_bounds__(A::kMaxThreads, 1) col_kernel(ColArgs a)
+{
+    using T = typename A::T;
+    using S = typename A::S;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cpx<T> *s = reinterpret_cast<cpx<T> *>(smem_raw);
+    __shared__ int sE[16], sEc[16];
+    const int log2W = a.log2W, W = 1 << log2W, wmask = W - 1;
+    const int L = a.nx / C;
+    unsigned crank = 0;
+    if constexpr (C > 1) crank = cg::this_cluster().block_rank();
+    const int col0 = (blockIdx.x / C) * W;
+    S *data = reinterpret_cast<S *>(a.data) + (long long)blockIdx.y * a.bstride;
+    const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
+    const int tid = threadIdx.x, nth = blockDim.x, nel = L << log2W;
+
+    if constexpr (A::kScaled) {
+        if (tid < 16) sE[tid] = 0;
+        __syncthreads();
+        int emax = 0;
+        for (int t = tid; t < nel; t += nth) {
+            const int w = t & wmask, m = t >> log2W, col = col0 + w;
+            double2 v = make_double2(0.0, 0.0);
+            if (col < a.ncols) {
+                const long long n = crank + (long long)C * m;
+                v = *reinterpret_cast<const double2 *>(data + n * a.row_stride + 2 * (long long)col);
+            }
+            reinterpret_cast<double2 *>(s)[t] = v;
+            emax = max(emax, max(dbl_biased_exp(v.x), dbl_biased_exp(v.y)));
+        }
+        reduce_exponents<C>(emax, log2W, sE, sEc);
+        for (int t = tid; t < nel; t += nth) {
+            const double2 v = reinterpret_cast<double2 *>(s)[t];
+            const int E = scale_exp(sEc[t & wmask]);
+            s[t] = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
+        }
+    } else {
+        for (int t = tid; t < nel; t += nth) {
+            const int w = t & wmask, m = t >> log2W, col = col0 + w;
+            cpx<T> v = czero<T>();
+            if (col < a.ncols)
+                v = load_c<A>(data + (crank + (long long)C * m) * a.row_stride + 2 * (long long)col, 0);
+            s[t] = v;
+        }
+    }
+    __syncthreads();
+
+    local_fft<T, DIR>(s, L, log2W, a.pp, tw, a.Ltab);
+
+    if constexpr (C == 1) {
+        for (int t = tid; t < nel; t += nth) {
+            const int w = t & wmask, k = t >> log2W, col = col0 + w;
+            if (col >= a.ncols) continue;
+            const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
+            store_c<A>(data + (long long)k * a.row_stride + 2 * (long long)col, s[t], E);
+        }
+    } else {
+        cg::cluster_group cl = cg::this_cluster();
+        if (crank > 0)
+            for (int t = tid; t < nel; t += nth) {
+                const int k2 = t >> log2W;
+                s[t] = cnorm(cmul(s[t], twid<DIR>(tw, (int)crank * k2)));
+            }
+        cl.sync();
+        const int Lc = L / C, k20 = crank * Lc;
+        const int ntask = Lc << log2W;
+        for (int t = tid; t < ntask; t += nth) {
+            const int w = t & wmask, k2 = k20 + (t >> log2W), col = col0 + w;
+            cpx<T> v[C];
+#pragma unroll
+            for (int r = 0; r < C; ++r) v[r] = *cl.map_shared_rank(&s[(k2 << log2W) + w], r);
+            DFT<C, DIR, T>::run(v);
+            if (col < a.ncols) {
+                const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
+#pragma unroll
+                for (int k1 = 0; k1 < C; ++k1)
+                    store_c<A>(data + (long long)(k2 + L * k1) * a.row_stride + 2 * (long long)col, v[k1], E);
+            }
+        }
+        cl.sync();
+    }
+}
+
+// --------------------------------------------------------- twiddle tables
+// W_N^e = exp(-2 pi i e / N) from FP64 sincospi, rounded once to the compute
+// type (float-float keeps 48 of its 53 bits).
+template <class T>
+__global__ void twiddle_kernel(cpx<T> *tab, int N)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= N) return;
+    double sn, cs;
+    sincospi(2.0 * (double)e / (double)N, &sn, &cs);
+    const double re = cs, im = -sn;
+    if constexpr (std::is_same<T, ff>::value) {
+        ff r, i;
+        r.hi = (float)re;
+        r.lo = (float)(re - (double)r.hi);
+        i.hi = (float)im;
+        i.lo = (float)(im - (double)i.hi);
+        tab[e] = cpx<ff>{r, i};
+    } else {
+        tab[e] = cpx<T>{(T)re, (T)im};
+    }
+}
+
+}  // namespace hpxfft_gpu

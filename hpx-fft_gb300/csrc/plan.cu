@@ -1,0 +1,599 @@
+// Plan construction and the C ABI (include/hpxfft_gb300.h).
+//
+// A plan mirrors what hpxfft::shared::loop::initialize builds
+// (core/src/shared/loop.cpp:158-189): the dimensions derived from the padded
+// buffer (dim_c_x = n_row, dim_c_y = n_col/2, dim_r_y = 2*dim_c_y - 2), one
+// row plan and one column plan.  Instead of FFTW plans it holds the launch
+// shapes of the two kernels, their radix sequences and FP64-generated
+// twiddle tables in HBM.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <vector>
+#include <string>
+
+#include "../../include/hpxfft_gb300.h"
+#include "launch.cuh"
+
+namespace hpxfft_gpu {
+
+static thread_local std::string g_last_error;
+
+static int fail(int status, const std::string &msg)
+{
+    g_last_error = msg;
+    return status;
+}
+static int cuda_fail(cudaError_t e, const char *what)
+{
+    return fail(HPXFFT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+struct DimPlan {
+    LaunchShape shape{};
+    PassPlan pp{};
+    int C = 1;
+    int log2W = 0;
+    int L = 0;
+};
+
+}  // namespace hpxfft_gpu
+
+struct hpxfft_plan_s {
+    size_t nx = 0, ny = 0, M = 0, dcy = 0, ncol = 0, batch = 1;
+    int prec = HPXFFT_PREC_F64;
+    std::string flag;
+    size_t real_bytes = 8;  // bytes of one storage real
+    size_t tw_elem = 16;    // bytes of one complex twiddle
+    hpxfft_gpu::DimPlan row, col;
+    void *tw_row = nullptr, *tw_col = nullptr;
+    void *dbuf = nullptr;
+    size_t dbuf_bytes = 0;
+    cudaStream_t own_stream = nullptr, stream = nullptr;
+    // kernel timing ring: slot i holds events before the first kernel, between
+    // the two kernels and after the second; slots [done, next) are unread
+    static constexpr int kSlots = 64;
+    cudaEvent_t kev[kSlots][3] = {};
+    long long next = 0, done = 0;
+    cudaEvent_t ev_copy[2] = {};  // before the host->device copy, after the device->host copy
+    bool pending_copy = false;
+    double sum_first = 0, sum_second = 0, sum_total = 0;
+    long long nsum = 0;
+    std::map<std::string, double> meas;
+};
+
+namespace hpxfft_gpu {
+
+// radix sequence for a local length L: 16s first, then the power-of-two
+// remainder, then 3s and 5s
+static bool factorize(int L, int max_radix, PassPlan &pp)
+{
+    pp.n = 0;
+    int rest = L;
+    int p3 = 0, p5 = 0;
+    while (rest % 3 == 0) rest /= 3, ++p3;
+    while (rest % 5 == 0) rest /= 5, ++p5;
+    if (rest & (rest - 1)) return false;  // a factor other than 2, 3, 5
+    int p2 = 0;
+    while ((1 << p2) < rest) ++p2;
+    const int lmax = max_radix == 16 ? 4 : 3;
+    std::vector<int> r;
+    while (p2 >= lmax) r.push_back(1 << lmax), p2 -= lmax;
+    if (p2 > 0) r.push_back(1 << p2);
+    for (int i = 0; i < p3; ++i) r.push_back(3);
+    for (int i = 0; i < p5; ++i) r.push_back(5);
+    if ((int)r.size() > kMaxPasses) return false;
+    pp.n = (int)r.size();
+    for (size_t i = 0; i < r.size(); ++i) pp.radix[i] = r[i];
+    return true;
+}
+
+static int max_threads_for(int prec) { return prec == HPXFFT_PREC_F32 ? 1024 : 512; }
+
+static int threads_for(int nel)
+{
+    int t = (nel + kElemsPerThread - 1) / kElemsPerThread;
+    t = (t + 31) / 32 * 32;
+    return t < 32 ? 32 : t;
+}
+
+static bool plan_rows(hpxfft_plan_s &p)
+{
+    const int maxel = kElemsPerThread * max_threads_for(p.prec);
+    const size_t cbytes = 2 * p.real_bytes;
+    for (int C : {1, 2, 4}) {
+        if (p.M % C) continue;
+        const int L = (int)(p.M / C);
+        if (C > 1 && L % C) continue;
+        if (L > maxel) continue;
+        PassPlan pp;
+        if (!factorize(L, 16, pp)) return false;
+        int log2W = 0;
+        if (C == 1)
+            while (log2W < 4 && (L << (log2W + 1)) <= 4096 && ((size_t)1 << log2W) < p.nx) ++log2W;
+        DimPlan &d = p.row;
+        d.C = C;
+        d.L = L;
+        d.log2W = log2W;
+        d.pp = pp;
+        const int nel = L << log2W;
+        d.shape.threads = threads_for(nel);
+        d.shape.smem = (size_t)nel * cbytes;
+        d.shape.cluster = C;
+        const size_t groups = (p.nx + ((size_t)1 << log2W) - 1) >> log2W;
+        d.shape.grid = dim3((unsigned)(groups * C), (unsigned)p.batch, 1);
+        return true;
+    }
+    return false;
+}
+
+static bool plan_cols(hpxfft_plan_s &p)
+{
+    const int maxel = kElemsPerThread * max_threads_for(p.prec);
+    const size_t cbytes = 2 * p.real_bytes;
+    int log2W = p.prec == HPXFFT_PREC_F32 ? 3 : 2;  // 64-byte row segments
+    while (log2W > 0 && ((size_t)1 << (log2W - 1)) >= p.dcy) --log2W;
+    for (int C : {1, 2, 4, 8, 16}) {
+        if (p.nx % C) continue;
+        const int L = (int)(p.nx / C);
+        if (C > 1 && L % C) continue;
+        if ((L << log2W) > maxel) continue;
+        PassPlan pp;
+        if (!factorize(L, 16, pp)) return false;
+        DimPlan &d = p.col;
+        d.C = C;
+        d.L = L;
+        d.log2W = log2W;
+        d.pp = pp;
+        const int nel = L << log2W;
+        d.shape.threads = threads_for(nel);
+        d.shape.smem = (size_t)nel * cbytes;
+        d.shape.cluster = C;
+        const size_t strips = (p.dcy + ((size_t)1 << log2W) - 1) >> log2W;
+        d.shape.grid = dim3((unsigned)(strips * C), (unsigned)p.batch, 1);
+        return true;
+    }
+    return false;
+}
+
+template <class A>
+static cudaError_t prepare_once()
+{
+    static cudaError_t status = Launch<A>::prepare();
+    return status;
+}
+
+static cudaError_t prepare_prec(int prec)
+{
+    switch (prec) {
+    case HPXFFT_PREC_F64: return prepare_once<ArithFF>();
+    case HPXFFT_PREC_F64_NATIVE: return prepare_once<ArithF64>();
+    default: return prepare_once<ArithF32>();
+    }
+}
+
+static cudaError_t gen_twiddles(int prec, void *tab, int n, cudaStream_t st)
+{
+    switch (prec) {
+    case HPXFFT_PREC_F64: return Launch<ArithFF>::twiddles(tab, n, st);
+    case HPXFFT_PREC_F64_NATIVE: return Launch<ArithF64>::twiddles(tab, n, st);
+    default: return Launch<ArithF32>::twiddles(tab, n, st);
+    }
+}
+
+static RowArgs row_args(const hpxfft_plan_s &p, const void *in, void *out, int adjoint)
+{
+    RowArgs a{};
+    a.in = in;
+    a.out = out;
+    a.in_stride = (long long)p.ncol;
+    a.out_stride = (long long)p.ncol;
+    a.in_bstride = (long long)(p.nx * p.ncol);
+    a.out_bstride = (long long)(p.nx * p.ncol);
+    a.nrows = (int)p.nx;
+    a.M = (int)p.M;
+    a.log2W = p.row.log2W;
+    a.adjoint = adjoint;
+    a.pp = p.row.pp;
+    a.tw = p.tw_row;
+    a.Ltab = (int)(2 * p.M);
+    return a;
+}
+
+static ColArgs col_args(const hpxfft_plan_s &p, void *data)
+{
+    ColArgs a{};
+    a.data = data;
+    a.row_stride = (long long)p.ncol;
+    a.bstride = (long long)(p.nx * p.ncol);
+    a.nx = (int)p.nx;
+    a.ncols = (int)p.dcy;
+    a.log2W = p.col.log2W;
+    a.pp = p.col.pp;
+    a.tw = p.tw_col;
+    a.Ltab = (int)p.nx;
+    return a;
+}
+
+static int collect(hpxfft_plan_s &p);
+
+// Events of the next timing slot; reads back the oldest slot when all are in flight.
+static cudaEvent_t *next_slot(hpxfft_plan_s &p)
+{
+    if (p.next - p.done >= hpxfft_plan_s::kSlots) {
+        const long long keep = p.next;
+        p.next = p.done + 1;  // collect exactly the oldest slot
+        collect(p);
+        p.next = keep;
+    }
+    return p.kev[p.next % hpxfft_plan_s::kSlots];
+}
+
+template <class A>
+static cudaError_t run_forward(hpxfft_plan_s &p, const void *in, void *out)
+{
+    cudaError_t e;
+    cudaEvent_t *ev = next_slot(p);
+    if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
+    if ((e = Launch<A>::row_r2c(row_args(p, in, out, 0), p.row.shape, p.stream)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
+    if ((e = Launch<A>::col(col_args(p, out), -1, p.col.shape, p.stream)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(ev[2], p.stream)) != cudaSuccess) return e;
+    ++p.next;
+    return cudaSuccess;
+}
+
+template <class A>
+static cudaError_t run_inverse(hpxfft_plan_s &p, void *data, int adjoint)
+{
+    cudaError_t e;
+    cudaEvent_t *ev = next_slot(p);
+    if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
+    if ((e = Launch<A>::col(col_args(p, data), +1, p.col.shape, p.stream)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
+    if ((e = Launch<A>::row_c2r(row_args(p, data, data, adjoint), p.row.shape, p.stream)) != cudaSuccess)
+        return e;
+    if ((e = cudaEventRecord(ev[2], p.stream)) != cudaSuccess) return e;
+    ++p.next;
+    return cudaSuccess;
+}
+
+static cudaError_t dispatch_forward(hpxfft_plan_s &p, const void *in, void *out)
+{
+    switch (p.prec) {
+    case HPXFFT_PREC_F64: return run_forward<ArithFF>(p, in, out);
+    case HPXFFT_PREC_F64_NATIVE: return run_forward<ArithF64>(p, in, out);
+    default: return run_forward<ArithF32>(p, in, out);
+    }
+}
+
+static cudaError_t dispatch_inverse(hpxfft_plan_s &p, void *data, int adjoint)
+{
+    switch (p.prec) {
+    case HPXFFT_PREC_F64: return run_inverse<ArithFF>(p, data, adjoint);
+    case HPXFFT_PREC_F64_NATIVE: return run_inverse<ArithF64>(p, data, adjoint);
+    default: return run_inverse<ArithF32>(p, data, adjoint);
+    }
+}
+
+// Read back every unread timing slot (blocks until those transforms are
+// done).  The per-key measurements describe the most recent transform, like
+// the reference's measurements_ map; the sums feed hpxfft_timing_stats.
+static int collect(hpxfft_plan_s &p)
+{
+    const int K = hpxfft_plan_s::kSlots;
+    for (; p.done < p.next; ++p.done) {
+        cudaEvent_t *ev = p.kev[p.done % K];
+        cudaError_t e = cudaEventSynchronize(ev[2]);
+        if (e != cudaSuccess) return cuda_fail(e, "transform");
+        float a = 0, b = 0, c = 0;
+        cudaEventElapsedTime(&a, ev[0], ev[1]);
+        cudaEventElapsedTime(&b, ev[1], ev[2]);
+        cudaEventElapsedTime(&c, ev[0], ev[2]);
+        p.sum_first += 1e-3 * a;
+        p.sum_second += 1e-3 * b;
+        p.sum_total += 1e-3 * c;
+        ++p.nsum;
+        p.meas["first_fftw"] = 1e-3 * a;
+        p.meas["first_trans"] = 0.0;
+        p.meas["second_fftw"] = 1e-3 * b;
+        p.meas["second_trans"] = 0.0;
+        p.meas["total"] = 1e-3 * c;
+        const double bytes = 4.0 * (double)(p.nx * p.dcy * 2 * p.real_bytes) * (double)p.batch;
+        p.meas["gbps"] = c > 0 ? bytes / (1e-3 * c) / 1e9 : 0.0;
+        if (p.done + 1 == p.next && p.pending_copy) {
+            float h = 0, d = 0, t = 0;
+            cudaEventElapsedTime(&h, p.ev_copy[0], ev[0]);
+            cudaEventElapsedTime(&d, ev[2], p.ev_copy[1]);
+            cudaEventElapsedTime(&t, p.ev_copy[0], p.ev_copy[1]);
+            p.meas["h2d"] = 1e-3 * h;
+            p.meas["d2h"] = 1e-3 * d;
+            p.meas["e2e"] = 1e-3 * t;
+            p.pending_copy = false;
+        }
+    }
+    return HPXFFT_OK;
+}
+
+static bool valid_flag(const char *f)
+{
+    if (!f) return false;
+    return !strcmp(f, "estimate") || !strcmp(f, "measure") || !strcmp(f, "patient") || !strcmp(f, "exhaustive");
+}
+
+static std::string describe(const hpxfft_plan_s &p, const DimPlan &d, const char *what, size_t len)
+{
+    char buf[512];
+    std::string radices;
+    for (int i = 0; i < d.pp.n; ++i) radices += (i ? "x" : "") + std::to_string(d.pp.radix[i]);
+    if (radices.empty()) radices = "1";
+    snprintf(buf, sizeof(buf),
+             "(gpu-%s n=%zu cluster=%d local=%d radices=%s interleaved=%d grid=%ux%u threads=%d smem=%zu "
+             "precision=%s)",
+             what, len, d.C, d.L, radices.c_str(), 1 << d.log2W, d.shape.grid.x, d.shape.grid.y, d.shape.threads,
+             d.shape.smem,
+             p.prec == HPXFFT_PREC_F64 ? "f64-floatfloat" : (p.prec == HPXFFT_PREC_F64_NATIVE ? "f64-dfma" : "f32"));
+    return buf;
+}
+
+}  // namespace hpxfft_gpu
+
+using namespace hpxfft_gpu;
+
+extern "C" {
+
+const char *hpxfft_status_string(int s)
+{
+    switch (s) {
+    case HPXFFT_OK: return "ok";
+    case HPXFFT_ERR_INVALID_ARG: return "invalid argument";
+    case HPXFFT_ERR_UNSUPPORTED_SIZE: return "unsupported size";
+    case HPXFFT_ERR_ALLOC: return "allocation failed";
+    case HPXFFT_ERR_CUDA: return "CUDA error";
+    case HPXFFT_ERR_TIMEOUT: return "device wait timed out";
+    case HPXFFT_ERR_STATE: return "invalid state";
+    case HPXFFT_ERR_IO: return "file I/O error";
+    default: return "unknown status";
+    }
+}
+
+const char *hpxfft_last_error(void) { return g_last_error.c_str(); }
+
+int hpxfft_plan_flag_valid(const char *plan_flag) { return valid_flag(plan_flag) ? 1 : 0; }
+
+int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batch, int precision,
+                       const char *plan_flag)
+{
+    if (!out) return fail(HPXFFT_ERR_INVALID_ARG, "plan pointer is null");
+    *out = nullptr;
+    if (!valid_flag(plan_flag)) return fail(HPXFFT_ERR_INVALID_ARG, "Invalid FFTW plan flag string");
+    if (precision < HPXFFT_PREC_F64 || precision > HPXFFT_PREC_F32)
+        return fail(HPXFFT_ERR_INVALID_ARG, "unknown precision");
+    if (n_row == 0 || batch == 0) return fail(HPXFFT_ERR_INVALID_ARG, "empty array");
+    if (n_col < 4 || n_col % 2) return fail(HPXFFT_ERR_UNSUPPORTED_SIZE, "n_col must be 2*(ny/2+1) with ny >= 2 even");
+    if (n_row > (1u << 30) || n_col > (1u << 30) || batch > 65535)
+        return fail(HPXFFT_ERR_UNSUPPORTED_SIZE, "dimension too large");
+    const auto t0 = std::chrono::steady_clock::now();
+    hpxfft_plan_s *p = new (std::nothrow) hpxfft_plan_s();
+    if (!p) return fail(HPXFFT_ERR_ALLOC, "host allocation failed");
+    p->nx = n_row;
+    p->dcy = n_col / 2;     // loop.cpp:164
+    p->ny = 2 * p->dcy - 2; // loop.cpp:165
+    p->M = p->ny / 2;
+    p->ncol = n_col;
+    p->batch = batch;
+    p->prec = precision;
+    p->flag = plan_flag;
+    p->real_bytes = precision == HPXFFT_PREC_F32 ? 4 : 8;
+    p->tw_elem = precision == HPXFFT_PREC_F32 ? 8 : 16;
+    if (!plan_rows(*p) || !plan_cols(*p)) {
+        delete p;
+        return fail(HPXFFT_ERR_UNSUPPORTED_SIZE,
+                    "sizes must factor into 2, 3 and 5 and fit the per-cluster shared memory");
+    }
+    cudaError_t e = prepare_prec(precision);
+    if (e != cudaSuccess) {
+        delete p;
+        return cuda_fail(e, "kernel attributes");
+    }
+    if ((e = cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        delete p;
+        return cuda_fail(e, "stream");
+    }
+    p->stream = p->own_stream;
+    for (auto &slot : p->kev)
+        for (auto &ev : slot)
+            if ((e = cudaEventCreate(&ev)) != cudaSuccess) {
+                hpxfft_plan_destroy(p);
+                return cuda_fail(e, "event");
+            }
+    for (auto &ev : p->ev_copy)
+        if ((e = cudaEventCreate(&ev)) != cudaSuccess) {
+            hpxfft_plan_destroy(p);
+            return cuda_fail(e, "event");
+        }
+    if (cudaMalloc(&p->tw_row, p->tw_elem * 2 * p->M) != cudaSuccess ||
+        cudaMalloc(&p->tw_col, p->tw_elem * p->nx) != cudaSuccess) {
+        hpxfft_plan_destroy(p);
+        return fail(HPXFFT_ERR_ALLOC, "twiddle tables");
+    }
+    if ((e = gen_twiddles(precision, p->tw_row, (int)(2 * p->M), p->stream)) != cudaSuccess ||
+        (e = gen_twiddles(precision, p->tw_col, (int)p->nx, p->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(p->stream)) != cudaSuccess) {
+        hpxfft_plan_destroy(p);
+        return cuda_fail(e, "twiddle generation");
+    }
+    const auto t1 = std::chrono::steady_clock::now();
+    p->meas["plan"] = std::chrono::duration<double>(t1 - t0).count();
+    // loop.cpp:188 counts dim_r_y r2c plans and dim_c_x c2c plans; keep that
+    // formula for the key, with 2.5 n log2 n per r2c and 5 n log2 n per c2c
+    const double ny = (double)p->ny, nx = (double)p->nx;
+    const double f_r2c = 2.5 * ny * std::log2(ny), f_c2c = nx > 1 ? 5.0 * nx * std::log2(nx) : 0.0;
+    p->meas["plan_flops"] = ny * f_r2c + nx * f_c2c;
+    p->meas["plan_flops_actual"] = (nx * f_r2c + (double)p->dcy * f_c2c) * (double)batch;
+    *out = p;
+    return HPXFFT_OK;
+}
+
+int hpxfft_plan_destroy(hpxfft_plan p)
+{
+    if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    cudaFree(p->tw_row);
+    cudaFree(p->tw_col);
+    cudaFree(p->dbuf);
+    for (auto &slot : p->kev)
+        for (auto &ev : slot)
+            if (ev) cudaEventDestroy(ev);
+    for (auto &ev : p->ev_copy)
+        if (ev) cudaEventDestroy(ev);
+    if (p->own_stream) cudaStreamDestroy(p->own_stream);
+    delete p;
+    return HPXFFT_OK;
+}
+
+int hpxfft_plan_set_stream(hpxfft_plan p, void *stream)
+{
+    if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
+    p->stream = stream ? (cudaStream_t)stream : p->own_stream;
+    return HPXFFT_OK;
+}
+
+int hpxfft_plan_buffer_bytes(hpxfft_plan p, size_t *bytes)
+{
+    if (!p || !bytes) return fail(HPXFFT_ERR_INVALID_ARG, "null argument");
+    *bytes = p->nx * p->ncol * p->real_bytes * p->batch;
+    return HPXFFT_OK;
+}
+
+int hpxfft_execute_r2c_oop(hpxfft_plan p, const void *d_in, void *d_out)
+{
+    if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
+    if (!d_in || !d_out) return fail(HPXFFT_ERR_INVALID_ARG, "null device buffer");
+    if (((uintptr_t)d_in | (uintptr_t)d_out) & 15) return fail(HPXFFT_ERR_INVALID_ARG, "buffers must be 16-byte aligned");
+    cudaError_t e = dispatch_forward(*p, d_in, d_out);
+    if (e != cudaSuccess) return cuda_fail(e, "forward launch");
+    return HPXFFT_OK;
+}
+
+int hpxfft_execute_r2c(hpxfft_plan p, void *d) { return hpxfft_execute_r2c_oop(p, d, d); }
+
+static int ensure_dbuf(hpxfft_plan p)
+{
+    size_t bytes = p->nx * p->ncol * p->real_bytes * p->batch;
+    if (p->dbuf && p->dbuf_bytes >= bytes) return HPXFFT_OK;
+    cudaFree(p->dbuf);
+    p->dbuf = nullptr;
+    if (cudaMalloc(&p->dbuf, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(HPXFFT_ERR_ALLOC, "device buffer");
+    }
+    p->dbuf_bytes = bytes;
+    return HPXFFT_OK;
+}
+
+int hpxfft_execute_r2c_host(hpxfft_plan p, void *h)
+{
+    if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
+    if (!h) return fail(HPXFFT_ERR_INVALID_ARG, "null host buffer");
+    int rc = ensure_dbuf(p);
+    if (rc) return rc;
+    const size_t bytes = p->nx * p->ncol * p->real_bytes * p->batch;
+    cudaError_t e;
+    if ((rc = collect(*p)) != HPXFFT_OK) return rc;
+    if ((e = cudaEventRecord(p->ev_copy[0], p->stream)) != cudaSuccess) return cuda_fail(e, "event");
+    if ((e = cudaMemcpyAsync(p->dbuf, h, bytes, cudaMemcpyHostToDevice, p->stream)) != cudaSuccess)
+        return cuda_fail(e, "host to device copy");
+    if ((e = dispatch_forward(*p, p->dbuf, p->dbuf)) != cudaSuccess) return cuda_fail(e, "forward launch");
+    if ((e = cudaMemcpyAsync(h, p->dbuf, bytes, cudaMemcpyDeviceToHost, p->stream)) != cudaSuccess)
+        return cuda_fail(e, "device to host copy");
+    if ((e = cudaEventRecord(p->ev_copy[1], p->stream)) != cudaSuccess) return cuda_fail(e, "event");
+    if ((e = cudaEventSynchronize(p->ev_copy[1])) != cudaSuccess) return cuda_fail(e, "transform");
+    p->pending_copy = true;
+    return collect(*p);
+}
+
+int hpxfft_execute_c2r(hpxfft_plan p, void *d)
+{
+    if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
+    if (!d) return fail(HPXFFT_ERR_INVALID_ARG, "null device buffer");
+    cudaError_t e = dispatch_inverse(*p, d, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "inverse launch");
+    return HPXFFT_OK;
+}
+
+int hpxfft_execute_r2c_backward(hpxfft_plan p, void *d)
+{
+    if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
+    if (!d) return fail(HPXFFT_ERR_INVALID_ARG, "null device buffer");
+    cudaError_t e = dispatch_inverse(*p, d, 1);
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
+    return HPXFFT_OK;
+}
+
+int hpxfft_get_measurement(hpxfft_plan p, const char *name, double *value)
+{
+    if (!p || !name || !value) return fail(HPXFFT_ERR_INVALID_ARG, "null argument");
+    int rc = collect(*p);
+    if (rc) return rc;
+    auto it = p->meas.find(name);
+    *value = it == p->meas.end() ? 0.0 : it->second;
+    return HPXFFT_OK;
+}
+
+int hpxfft_timing_stats(hpxfft_plan p, double *first_mean, double *second_mean, double *total_mean,
+                        long long *count)
+{
+    if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
+    int rc = collect(*p);
+    if (rc) return rc;
+    const double n = p->nsum ? (double)p->nsum : 1.0;
+    if (first_mean) *first_mean = p->sum_first / n;
+    if (second_mean) *second_mean = p->sum_second / n;
+    if (total_mean) *total_mean = p->sum_total / n;
+    if (count) *count = p->nsum;
+    return HPXFFT_OK;
+}
+
+int hpxfft_timing_reset(hpxfft_plan p)
+{
+    if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
+    int rc = collect(*p);
+    p->sum_first = p->sum_second = p->sum_total = 0.0;
+    p->nsum = 0;
+    return rc;
+}
+
+int hpxfft_write_plan(hpxfft_plan p, const char *path)
+{
+    if (!p || !path) return fail(HPXFFT_ERR_INVALID_ARG, "null argument");
+    FILE *f = fopen(path, "a");
+    if (!f) return fail(HPXFFT_ERR_IO, std::string("Failed to open file: ") + path);
+    fprintf(f, "GPU r2c 1D plan:\n%s\n", describe(*p, p->row, "r2c", p->ny).c_str());
+    fprintf(f, "GPU c2c 1D plan:\n%s\n\n", describe(*p, p->col, "c2c", p->nx).c_str());
+    fclose(f);
+    return HPXFFT_OK;
+}
+
+int hpxfft_host_alloc(void **ptr, size_t bytes)
+{
+    if (!ptr) return fail(HPXFFT_ERR_INVALID_ARG, "null argument");
+    if (cudaHostAlloc(ptr, bytes ? bytes : 1, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return fail(HPXFFT_ERR_ALLOC, "pinned host allocation");
+    }
+    return HPXFFT_OK;
+}
+
+int hpxfft_host_free(void *ptr)
+{
+    if (ptr && cudaFreeHost(ptr) != cudaSuccess) return fail(HPXFFT_ERR_CUDA, "cudaFreeHost");
+    return HPXFFT_OK;
+}
+
+}  // extern "C"

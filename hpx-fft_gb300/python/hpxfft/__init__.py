@@ -1,0 +1,18 @@
+"""Python mirror of the HPX-FFT API over the GB300 C ABI.
+
+Names and semantics follow the reference's C++ interface so that code and
+tests written against it read the same:
+
+  hpxfft.util.vector_2d            core/include/hpxfft/util/vector_2d.hpp:9-86
+  hpxfft.shared.loop               core/include/hpxfft/shared/loop.hpp:15-31
+  hpxfft.shared.naive/sync/opt     core/include/hpxfft/shared/{naive,sync,opt}.hpp
+  hpxfft.distributed.loop          core/include/hpxfft/distributed/loop.hpp:17-31
+
+Every transform runs in libhpxfft_gb300.so on the GPU; there is no CPU path.
+"""
+from . import _capi
+from ._capi import HpxFftError, HpxFftInvalidArgument
+from .plan import Plan
+from . import util, shared, distributed
+
+__all__ = ["Plan", "HpxFftError", "HpxFftInvalidArgument", "util", "shared", "distributed", "_capi"]

@@ -1,0 +1,139 @@
+/*
+ * hpxfft_gb300 -- C ABI of the GB300 (sm_103a) 2D real-to-complex FFT.
+ *
+ * This is the boundary the C++ drop-in headers (hpxfft::shared::loop and
+ * friends) and any FFI (ctypes, cgo, JNI) bind.  Plain pointers and sizes
+ * only; every function returns an hpxfft_status (0 = success).
+ *
+ * Data layout (the reference's, core/include/hpxfft/util/vector_2d.hpp:9-86
+ * and examples/hpxfft/shared_loop_2d.cpp:27-40): a row-major buffer of
+ * n_row x n_col reals, n_col = 2 * (ny/2 + 1).  The first ny reals of a row
+ * are input data, the last two are padding.  The forward transform overwrites
+ * row kx with the n_col/2 complex values X[kx][ky] = sum_{x,y} v[x][y]
+ * exp(-2 pi i (kx x / n_row + ky y / ny)), unnormalised (numpy.fft.rfft2
+ * orientation: the reference transposes back at the end,
+ * core/src/shared/loop.cpp:94-102).
+ *
+ * Precision: HPXFFT_PREC_F64 stores doubles and computes in float-float on
+ * the FP32 pipes (about 48 significant bits; relative L2 error vs FP64 FFTW
+ * is ~1e-14); HPXFFT_PREC_F64_NATIVE computes with DFMA (slow on GB300,
+ * kept as a cross-check); HPXFFT_PREC_F32 stores and computes float.
+ */
+#ifndef HPXFFT_GB300_H
+#define HPXFFT_GB300_H
+
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define HPXFFT_API __attribute__((visibility("default")))
+#else
+#define HPXFFT_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    HPXFFT_OK = 0,
+    HPXFFT_ERR_INVALID_ARG = 1,      /* std::invalid_argument in the reference (bad plan flag) */
+    HPXFFT_ERR_UNSUPPORTED_SIZE = 2, /* odd ny, a factor other than 2, 3, 5, too long a row */
+    HPXFFT_ERR_ALLOC = 3,            /* device or pinned allocation failed */
+    HPXFFT_ERR_CUDA = 4,             /* a CUDA runtime call failed */
+    HPXFFT_ERR_TIMEOUT = 5,          /* a bounded device-side wait gave up */
+    HPXFFT_ERR_STATE = 6,            /* call out of order (e.g. execute on a destroyed plan) */
+    HPXFFT_ERR_IO = 7                /* std::runtime_error in the reference (file open) */
+} hpxfft_status;
+
+typedef enum {
+    HPXFFT_PREC_F64 = 0,        /* FP64 in HBM, float-float arithmetic */
+    HPXFFT_PREC_F64_NATIVE = 1, /* FP64 in HBM, DFMA arithmetic */
+    HPXFFT_PREC_F32 = 2         /* FP32 in HBM and arithmetic */
+} hpxfft_precision;
+
+typedef struct hpxfft_plan_s *hpxfft_plan;
+
+/* Plan a 2D r2c of `batch` equally sized arrays of n_row x n_col reals
+ * (n_col = 2*(ny/2+1), so ny = n_col - 2).  plan_flag is one of
+ * "estimate", "measure", "patient", "exhaustive"; anything else returns
+ * HPXFFT_ERR_INVALID_ARG.  Allocates the twiddle tables and no data buffer.
+ * Replaces: hpxfft::shared::loop::initialize (core/src/shared/loop.cpp:158-189)
+ * and fftw_adapter::{r2c_1d,c2c_1d}::plan (core/src/util/adapter_fftw.cpp:6-10,24-30),
+ * string_to_fftw_plan_flag (core/include/hpxfft/util/adapter_fftw.hpp:22-44). */
+HPXFFT_API int hpxfft_plan_create(hpxfft_plan *plan, size_t n_row, size_t n_col, size_t batch, int precision,
+                       const char *plan_flag);
+
+/* Free the plan's device memory, events and owned stream.
+ * Replaces: ~loop / fftw_adapter::cleanup (core/include/hpxfft/shared/loop.hpp:30). */
+HPXFFT_API int hpxfft_plan_destroy(hpxfft_plan plan);
+
+/* Use a caller-owned cudaStream_t (NULL restores the plan's own stream). */
+HPXFFT_API int hpxfft_plan_set_stream(hpxfft_plan plan, void *cuda_stream);
+
+/* Bytes of one array in HBM (n_row * n_col * sizeof(real)) times batch. */
+HPXFFT_API int hpxfft_plan_buffer_bytes(hpxfft_plan plan, size_t *bytes);
+
+/* In-place forward transform of a device buffer in the padded layout,
+ * stream-ordered, asynchronous.  Replaces the four phases of
+ * loop::fft_2d_r2c_par (core/src/shared/loop.cpp:56-113) and the per-locality
+ * compute of distributed::loop::fft_2d_r2c at one locality
+ * (core/src/distributed/loop.cpp:130-272). */
+HPXFFT_API int hpxfft_execute_r2c(hpxfft_plan plan, void *device_values);
+
+/* Out-of-place forward transform: d_in (padded real layout, read only) to
+ * d_out (same layout, receives the spectrum).  d_in may equal d_out. */
+HPXFFT_API int hpxfft_execute_r2c_oop(hpxfft_plan plan, const void *d_in, void *d_out);
+
+/* Host buffer in, host buffer out (in place): copies to a plan-owned device
+ * buffer, transforms, copies back, synchronises.  The drop-in path of
+ * loop::initialize + loop::fft_2d_r2c_par. */
+HPXFFT_API int hpxfft_execute_r2c_host(hpxfft_plan plan, void *host_values);
+
+/* Unnormalised inverse (c2r) of a half spectrum in the padded layout, in
+ * place: nx*ny * original.  No reference counterpart (the FFTW backward
+ * direction exists in core/include/hpxfft/util/adapter_fftw.hpp:11 but is
+ * never planned). */
+HPXFFT_API int hpxfft_execute_c2r(hpxfft_plan plan, void *device_values);
+
+/* Adjoint of the forward transform, in place: the buffer holds G =
+ * dL/dRe X + i dL/dIm X over the half spectrum and receives dL/dx (pads 0).
+ * No reference counterpart (gradient for fft_2d_r2c_backward). */
+HPXFFT_API int hpxfft_execute_r2c_backward(hpxfft_plan plan, void *device_values);
+
+/* Measurement by key, seconds unless stated: "total", "first_fftw" (row
+ * kernel), "first_trans" (0: fused), "second_fftw" (column kernel),
+ * "second_trans" (0: fused), "plan", "plan_flops", "h2d", "d2h", "e2e"
+ * (host buffer in to host buffer out of the last hpxfft_execute_r2c_host).
+ * Unknown keys give 0, like loop::get_measurement (core/src/shared/loop.cpp:192). */
+HPXFFT_API int hpxfft_get_measurement(hpxfft_plan plan, const char *name, double *value);
+
+/* Mean kernel durations (seconds) over every transform executed since the
+ * last hpxfft_timing_reset: first = row kernel, second = column kernel (the
+ * inverse runs them in the opposite order), total = both.  Blocks until the
+ * transforms are done.  No reference counterpart (the reference keeps the
+ * last run only, core/src/shared/loop.cpp:106-110). */
+HPXFFT_API int hpxfft_timing_stats(hpxfft_plan plan, double *first_mean, double *second_mean, double *total_mean,
+                                   long long *count);
+HPXFFT_API int hpxfft_timing_reset(hpxfft_plan plan);
+
+/* Append the chosen GPU plan to a text file.  HPXFFT_ERR_IO if the file
+ * cannot be opened.  Replaces loop::write_plans_to_file
+ * (core/src/shared/loop.cpp:194-212). */
+HPXFFT_API int hpxfft_write_plan(hpxfft_plan plan, const char *file_path);
+
+/* 1 if plan_flag is a valid plan flag string, else 0. */
+HPXFFT_API int hpxfft_plan_flag_valid(const char *plan_flag);
+
+/* Static description of a status code; message of the calling thread's
+ * most recent failure. */
+HPXFFT_API const char *hpxfft_status_string(int status);
+HPXFFT_API const char *hpxfft_last_error(void);
+
+/* Pinned host memory for fast host<->device copies (cudaHostAlloc). */
+HPXFFT_API int hpxfft_host_alloc(void **ptr, size_t bytes);
+HPXFFT_API int hpxfft_host_free(void *ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,123 @@
+"""CPU-only checks: the C ABI library loads and exports its header, argument
+validation that never touches the GPU, the float-float conversions compiled
+for the host, and the Python mirror of vector_2d."""
+import ctypes
+import os
+import re
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(REPO, "include", "hpxfft_gb300.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^HPXFFT_API[^(]*?\b(hpxfft_[a-z0-9_]+)\s*\(", text, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol(gpu_lib):
+    lib = gpu_lib._capi.load()
+    names = declared_symbols()
+    assert len(names) >= 16
+    for name in names:
+        assert hasattr(lib, name), name
+    assert set(names) == set(gpu_lib._capi.SIGNATURES)
+
+
+def test_status_strings_and_flags(gpu_lib):
+    lib = gpu_lib._capi.load()
+    assert lib.hpxfft_status_string(0) == b"ok"
+    assert lib.hpxfft_status_string(7) == b"file I/O error"
+    for f in (b"estimate", b"measure", b"patient", b"exhaustive"):
+        assert lib.hpxfft_plan_flag_valid(f) == 1
+    for f in (b"", b"Estimate", b"fast", None):
+        assert lib.hpxfft_plan_flag_valid(f) == 0
+
+
+def test_plan_argument_errors_before_any_device_call(gpu_lib):
+    # string_to_fftw_plan_flag throws std::invalid_argument (adapter_fftw.hpp:42)
+    with pytest.raises(gpu_lib.HpxFftInvalidArgument, match="plan flag"):
+        gpu_lib.Plan(4, 6, 1, "f64", "wisdom")
+    with pytest.raises(gpu_lib.HpxFftError) as e:
+        gpu_lib.Plan(4, 5, 1, "f64", "estimate")  # odd n_col: ny must be even (loop.cpp:164-165)
+    assert e.value.status == gpu_lib._capi.HPXFFT_ERR_UNSUPPORTED_SIZE
+    with pytest.raises(gpu_lib.HpxFftInvalidArgument):
+        gpu_lib.Plan(0, 6, 1, "f64", "estimate")
+    with pytest.raises(gpu_lib.HpxFftInvalidArgument):
+        gpu_lib.Plan(4, 6, 1, "f16", "estimate")
+    lib = gpu_lib._capi.load()
+    h = ctypes.c_void_p()
+    assert lib.hpxfft_plan_create(None, 4, 6, 1, 0, b"estimate") == gpu_lib._capi.HPXFFT_ERR_INVALID_ARG
+    assert lib.hpxfft_plan_create(ctypes.byref(h), 4, 6, 0, 0, b"estimate") == gpu_lib._capi.HPXFFT_ERR_INVALID_ARG
+    assert lib.hpxfft_plan_destroy(None) == gpu_lib._capi.HPXFFT_ERR_STATE
+    assert lib.hpxfft_execute_r2c(None, None) == gpu_lib._capi.HPXFFT_ERR_STATE
+
+
+@pytest.fixture(scope="module")
+def ffhost(tmp_path_factory):
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("g++ not available")
+    out = tmp_path_factory.mktemp("ff") / "ffhost.so"
+    src = os.path.join(REPO, "tests", "cpp", "ff_host_check.cpp")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-o", str(out), src], check=True)
+    lib = ctypes.CDLL(str(out))
+    return lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def test_float_float_round_trip(ffhost):
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal(50000)
+    y = np.zeros_like(x)
+    for E in (-70, -3, 0, 1, 40):
+        xs = x * 2.0**E
+        ffhost.ff_roundtrip(_dp(xs), _dp(y), xs.size, E)
+        assert np.max(np.abs(y - xs) / np.abs(xs)) <= 2.0**-47
+
+
+def test_float_float_special_values(ffhost):
+    x = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 2.0**-1074, 1.5, -3.25])
+    y = np.zeros_like(x)
+    ffhost.ff_roundtrip(_dp(x), _dp(y), x.size, 0)
+    assert y[0] == 0 and y[1] == 0 and np.signbit(y[1])
+    assert y[2] == np.inf and y[3] == -np.inf and np.isnan(y[4])
+    assert y[5] == 0.0  # subnormal doubles flush (far below 2^-126 of any block scale)
+    assert y[6] == 1.5 and y[7] == -3.25
+
+
+def test_float_float_arithmetic(ffhost):
+    rng = np.random.default_rng(12)
+    a, b = rng.standard_normal(20000), rng.standard_normal(20000)
+    y = np.zeros_like(a)
+    for op, f in ((0, np.add), (1, np.subtract), (2, np.multiply)):
+        ffhost.ff_binop(_dp(a), _dp(b), _dp(y), a.size, op)
+        scale = np.abs(a) + np.abs(b) if op < 2 else np.abs(a * b)
+        assert np.max(np.abs(y - f(a, b)) / scale) < 2.0**-45
+
+
+def test_vector_2d_mirror(gpu_lib):
+    # test/src/test_vector_2d.cpp:6-33
+    v2 = gpu_lib.util.vector_2d
+    vec = v2(3, 3, 4.0)
+    assert vec.n_row() == 3 and vec.n_col() == 3 and vec(0, 0) == 4.0 and vec(2, 2) == 4.0 and vec.size() == 9
+    with pytest.raises(RuntimeError):
+        v2(3, 3, 1.0).at(3, 3)
+    assert v2(2, 2, 5.0) == v2(2, 2, 5.0)
+    assert not (v2(2, 2, 5.0) == v2(2, 2, 6.0))
+    moved = v2(2, 4, 1.0)
+    data = moved.take()
+    assert data.shape == (2, 4) and moved.size() == 0
+
+
+def test_distributed_comm_flag_is_validated(gpu_lib):
+    v = gpu_lib.util.vector_2d(4, 6, 0.0)
+    with pytest.raises(gpu_lib.HpxFftInvalidArgument, match="scatter or all_to_all"):
+        gpu_lib.distributed.loop().initialize(v, "broadcast", "estimate")
