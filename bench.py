@@ -44,31 +44,36 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=16384, help="nx = ny")
+    ap.add_argument("--nx", type=int, default=0, help="rows (overrides --n; profiling cases)")
+    ap.add_argument("--ny", type=int, default=0, help="columns (overrides --n; profiling cases)")
     ap.add_argument("--precision", default="f64", choices=["f64", "f32", "f64-native"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    args = ap.parse_args()
+    args.nx = args.nx or args.n
+    args.ny = args.ny or args.n
+    return args
 
 
-def workload_input(n: int, seed: int = 1234) -> np.ndarray:
+def workload_input(nx: int, ny: int, seed: int = 1234) -> np.ndarray:
     """uniform[-1,1) plus four integer-frequency sinusoids of amplitude 10,
-    in the padded n x 2*(n/2+1) layout (float64)."""
+    in the padded nx x 2*(ny/2+1) layout (float64)."""
     rng = np.random.default_rng(seed)
-    nc = 2 * (n // 2 + 1)
-    x = np.zeros((n, nc), dtype=np.float64)
-    x[:, :n] = rng.uniform(-1.0, 1.0, (n, n))
-    i = np.arange(n, dtype=np.float64)[:, None]
-    j = np.arange(n, dtype=np.float64)[None, :]
+    nc = 2 * (ny // 2 + 1)
+    x = np.zeros((nx, nc), dtype=np.float64)
+    x[:, :ny] = rng.uniform(-1.0, 1.0, (nx, ny))
+    i = np.arange(nx, dtype=np.float64)[:, None]
+    j = np.arange(ny, dtype=np.float64)[None, :]
     for _ in range(4):
-        fx, fy = rng.integers(1, n // 2, size=2)
-        # row by row to bound the temporary
-        for r0 in range(0, n, 1024):
-            x[r0:r0 + 1024, :n] += 10.0 * np.sin(2 * np.pi * (fx * i[r0:r0 + 1024] / n + fy * j / n))
+        fx, fy = rng.integers(1, max(2, min(nx, ny) // 2), size=2)
+        # 1024 rows at a time to bound the temporary
+        for r0 in range(0, nx, 1024):
+            x[r0:r0 + 1024, :ny] += 10.0 * np.sin(2 * np.pi * (fx * i[r0:r0 + 1024] / nx + fy * j / ny))
     return x
 
 
-def algorithmic_bytes(n: int, real_bytes: int) -> float:
-    S = n * (n // 2 + 1) * 2 * real_bytes
+def algorithmic_bytes(nx: int, ny: int, real_bytes: int) -> float:
+    S = nx * (ny // 2 + 1) * 2 * real_bytes
     return 4.0 * S
 
 
@@ -141,7 +146,7 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(n: int, host_input: np.ndarray, threads: int) -> dict:
+def cpu_baseline(nx: int, ny: int, host_input: np.ndarray, threads: int) -> dict:
     """The oracle (FP64 C restatement of shared::loop) on the host cores, one
     full transform of the same input."""
     import oracle
@@ -151,11 +156,11 @@ def cpu_baseline(n: int, host_input: np.ndarray, threads: int) -> dict:
     oracle.fft_2d_r2c(work, nthreads=threads)
     dt = time.perf_counter() - t0
     return {
-        "value": algorithmic_bytes(n, 8) / dt / 1e9,
+        "value": algorithmic_bytes(nx, ny, 8) / dt / 1e9,
         "unit": UNIT,
         "cores": threads,
         "kind": "port",
-        "sample": f"one full {n}x{n} FP64 2D r2c ({dt:.2f} s) by the C restatement of hpxfft::shared::loop, "
+        "sample": f"one full {nx}x{ny} FP64 2D r2c ({dt:.2f} s) by the C restatement of hpxfft::shared::loop, "
                   f"{threads} threads; HPX and FFTW are not installed, so the reference binary cannot run",
         "seconds": dt,
     }
@@ -180,9 +185,9 @@ def run_reference(args):
     b.build_oracle()
     import oracle
 
-    n = args.n
+    nx, ny = args.nx, args.ny
     threads = os.cpu_count() or 1
-    x = workload_input(n)
+    x = workload_input(nx, ny)
     work = np.empty_like(x)
     for _ in range(args.warmup):
         np.copyto(work, x)
@@ -194,7 +199,7 @@ def run_reference(args):
         oracle.fft_2d_r2c(work, nthreads=threads)
         times.append(time.perf_counter() - t0)
     t = sum(times) / len(times)
-    value = algorithmic_bytes(n, 8) / t / 1e9
+    value = algorithmic_bytes(nx, ny, 8) / t / 1e9
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -209,10 +214,10 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic: uniform[-1,1) + 4 integer-frequency sinusoids of amplitude 10, seed 1234",
-        "config": {"workload": f"2d_r2c_fp64_{n}x{n}", "nx": n, "ny": n, "layout": "padded in-place vector_2d",
+        "config": {"workload": f"2d_r2c_fp64_{nx}x{ny}", "nx": nx, "ny": ny, "layout": "padded in-place vector_2d",
                    "implementation": "C restatement of hpxfft::shared::loop (FFTW/HPX unavailable)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} full {n}x{n} FP64 transforms, {threads} threads"},
+                         "sample": f"{args.steps} full {nx}x{ny} FP64 transforms, {threads} threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -240,16 +245,16 @@ def run_ours(args):
     b.build_all()
     import hpxfft
 
-    n = args.n
+    nx, ny = args.nx, args.ny
     prec = args.precision
     real_bytes = 4 if prec == "f32" else 8
-    nc = 2 * (n // 2 + 1)
-    x64 = workload_input(n, seed=1234 + rank)
+    nc = 2 * (ny // 2 + 1)
+    x64 = workload_input(nx, ny, seed=1234 + rank)
     host = x64.astype(np.float32) if prec == "f32" else x64
     dev_in = torch.from_numpy(host).cuda()
     dev_out = torch.empty_like(dev_in)
     stream = torch.cuda.current_stream()
-    plan = hpxfft.Plan(n, nc, 1, prec, "estimate")
+    plan = hpxfft.Plan(nx, nc, 1, prec, "estimate")
     plan.set_stream(stream.cuda_stream)
 
     # warm-up
@@ -279,7 +284,7 @@ def run_ours(args):
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
-    B = algorithmic_bytes(n, real_bytes)
+    B = algorithmic_bytes(nx, ny, real_bytes)
     value = world * B / (ms * 1e-3) / 1e9
 
     # accuracy of the timed output against the oracle on a bounded sample:
@@ -289,7 +294,7 @@ def run_ours(args):
     spec_out = out.view(np.complex128 if prec != "f32" else np.complex64)
 
     # end to end through the host-buffer C ABI call
-    pinned = torch.empty((n, nc), dtype=torch.float64 if prec != "f32" else torch.float32).pin_memory()
+    pinned = torch.empty((nx, nc), dtype=torch.float64 if prec != "f32" else torch.float32).pin_memory()
     host_src = torch.from_numpy(host)
     e2e_times = []
     for i in range(args.e2e_steps + 1):
@@ -315,7 +320,7 @@ def run_ours(args):
         cpu = None
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
-            cpu = cpu_baseline(n, x64, threads)
+            cpu = cpu_baseline(nx, ny, x64, threads)
             ref = x64.copy()
             oracle.fft_2d_r2c(ref, nthreads=threads)
             refc = ref.view(np.complex128)
@@ -334,8 +339,8 @@ def run_ours(args):
             "dtype": "f64" if prec != "f32" else "f32",
             "data": "synthetic: uniform[-1,1) + 4 integer-frequency sinusoids of amplitude 10, seed 1234+rank",
             "config": {
-                "workload": f"2d_r2c_{prec}_{n}x{n}",
-                "nx": n, "ny": n,
+                "workload": f"2d_r2c_{prec}_{nx}x{ny}",
+                "nx": nx, "ny": ny,
                 "precision": {"f64": "FP64 storage, float-float arithmetic", "f32": "FP32",
                               "f64-native": "FP64 storage, DFMA arithmetic"}[prec],
                 "layout": "padded vector_2d (n x 2*(n/2+1)), output [kx][ky]",
@@ -361,8 +366,8 @@ def run_ours(args):
             "e2e": {
                 "value": world * B / e2e_s / 1e9,
                 "unit": UNIT,
-                "h2d_bytes_per_step": int(n * nc * real_bytes),
-                "d2h_bytes_per_step": int(n * nc * real_bytes),
+                "h2d_bytes_per_step": int(nx * nc * real_bytes),
+                "d2h_bytes_per_step": int(nx * nc * real_bytes),
                 "ms_per_step": 1e3 * e2e_s,
                 "h2d_ms": 1e3 * h2d,
                 "d2h_ms": 1e3 * d2h,

@@ -24,7 +24,15 @@ ORACLE_LIB = os.path.join(ORACLE_BUILD, "libhpxfft_oracle.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden"]
-SOURCES = ["kernels_ff.cu", "kernels_f32.cu", "kernels_f64.cu", "plan.cu"]
+SOURCES = [
+    "kernels_ff_rows.cu",
+    "kernels_ff_cols.cu",
+    "kernels_f32_rows.cu",
+    "kernels_f32_cols.cu",
+    "kernels_f64.cu",
+    "twiddles.cu",
+    "plan.cu",
+]
 
 
 def _nvcc() -> str:

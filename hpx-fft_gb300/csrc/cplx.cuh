@@ -298,4 +298,109 @@ struct DFT<5, DIR, T> {
     }
 };
 
+// ------------------------------------------------------ odd prime radices
+#ifdef __CUDACC__
+#define HPXFFT_CONSTEXPR_HD constexpr __host__ __device__
+#else
+#define HPXFFT_CONSTEXPR_HD constexpr
+#endif
+// Compile-time cos / sin (Taylor series after reduction to |x| <= pi/4) so
+// the constants of the length-7, 11 and 13 butterflies are literals.
+constexpr long double kPiL = 3.141592653589793238462643383279502884L;
+HPXFFT_CONSTEXPR_HD long double taylor_sin(long double x)
+{
+    long double term = x, sum = x;
+    for (int k = 1; k < 16; ++k) {
+        term *= -x * x / ((2 * k) * (2 * k + 1));
+        sum += term;
+    }
+    return sum;
+}
+HPXFFT_CONSTEXPR_HD long double taylor_cos(long double x)
+{
+    long double term = 1, sum = 1;
+    for (int k = 1; k < 16; ++k) {
+        term *= -x * x / ((2 * k - 1) * (2 * k));
+        sum += term;
+    }
+    return sum;
+}
+// cos and sin of 2 pi m / n
+HPXFFT_CONSTEXPR_HD double cos2pi(int m, int n)
+{
+    m = ((m % n) + n) % n;
+    // octant reduction of the angle 2 pi m / n
+    const long double a = 2 * kPiL * (long double)m / (long double)n;
+    if (8 * m <= n) return (double)taylor_cos(a);
+    if (8 * m <= 3 * n) return (double)taylor_sin(kPiL / 2 - a);
+    if (8 * m <= 5 * n) return (double)(-taylor_cos(kPiL - a));
+    if (8 * m <= 7 * n) return (double)taylor_sin(a - 3 * kPiL / 2);
+    return (double)taylor_cos(2 * kPiL - a);
+}
+HPXFFT_CONSTEXPR_HD double sin2pi(int m, int n) { return cos2pi(4 * m - n, 4 * n); }  // sin(x) = cos(x - pi/2)
+
+// Constants of an odd-length butterfly, split into the compute type at
+// compile time: c[q][t] = cos(2 pi (q+1)(t+1) / R), s likewise.
+template <int R, class T>
+struct OddConsts {
+    T c[(R - 1) / 2][(R - 1) / 2];
+    T s[(R - 1) / 2][(R - 1) / 2];
+};
+template <int R, class T>
+HPXFFT_CONSTEXPR_HD OddConsts<R, T> make_odd_consts()
+{
+    OddConsts<R, T> k{};
+    for (int q = 0; q < (R - 1) / 2; ++q)
+        for (int t = 0; t < (R - 1) / 2; ++t) {
+            k.c[q][t] = real_ops<T>::cst(cos2pi((q + 1) * (t + 1), R));
+            k.s[q][t] = real_ops<T>::cst(sin2pi((q + 1) * (t + 1), R));
+        }
+    return k;
+}
+
+// Odd length R: pairs q, R-q share the real and imaginary sums
+//   X_t     = v0 + sum_q (v_q + v_{R-q}) cos(2 pi q t / R) + DIR i sum_q (v_q - v_{R-q}) sin(2 pi q t / R)
+//   X_{R-t} = same with the sine term negated.
+template <int R, int DIR, class T>
+struct DFTOdd {
+    static HPXFFT_HD void run(cpx<T> *v)
+    {
+        constexpr int H = (R - 1) / 2;
+        constexpr OddConsts<R, T> K = make_odd_consts<R, T>();
+        cpx<T> a[H], b[H];
+#pragma unroll
+        for (int q = 1; q <= H; ++q) {
+            a[q - 1] = v[q] + v[R - q];
+            b[q - 1] = v[q] - v[R - q];
+        }
+        cpx<T> out[R];
+        cpx<T> x0 = v[0];
+#pragma unroll
+        for (int q = 0; q < H; ++q) x0 = x0 + a[q];
+        out[0] = x0;
+#pragma unroll
+        for (int t = 1; t <= H; ++t) {
+            cpx<T> re = v[0], im = czero<T>();
+#pragma unroll
+            for (int q = 1; q <= H; ++q) {
+                const T c = K.c[q - 1][t - 1];
+                const T s = K.s[q - 1][t - 1];
+                re = cpx<T>{re.re + a[q - 1].re * c, re.im + a[q - 1].im * c};
+                im = cpx<T>{im.re + b[q - 1].re * s, im.im + b[q - 1].im * s};
+            }
+            const cpx<T> j = mul_i<DIR>(im);
+            out[t] = re + j;
+            out[R - t] = re - j;
+        }
+#pragma unroll
+        for (int t = 0; t < R; ++t) v[t] = out[t];
+    }
+};
+template <int DIR, class T>
+struct DFT<7, DIR, T> : DFTOdd<7, DIR, T> {};
+template <int DIR, class T>
+struct DFT<11, DIR, T> : DFTOdd<11, DIR, T> {};
+template <int DIR, class T>
+struct DFT<13, DIR, T> : DFTOdd<13, DIR, T> {};
+
 }  // namespace hpxfft_gpu

@@ -21,29 +21,33 @@ namespace hpxfft_gpu {
 namespace cg = cooperative_groups;
 
 constexpr int kMaxPasses = 24;
-// Radix sequence of one local Stockham transform (radices 2,3,4,5,8,16).
+// Radix sequence of one local Stockham transform (radices 2,3,4,5,7,8,11,13,16).
 struct PassPlan {
     int n;
     int radix[kMaxPasses];
 };
 
 // Compute-type traits: T = arithmetic type, S = storage (HBM) real type.
+// kFixedChains: compile-time pass chains are instantiated for this type.
 struct ArithF32 {
     using T = float;
     using S = float;
     static constexpr bool kScaled = false;
+    static constexpr bool kFixedChains = true;
     static constexpr int kMaxThreads = 1024;
 };
 struct ArithF64 {
     using T = double;
     using S = double;
     static constexpr bool kScaled = false;
+    static constexpr bool kFixedChains = false;
     static constexpr int kMaxThreads = 512;
 };
 struct ArithFF {
     using T = ff;
     using S = double;
     static constexpr bool kScaled = true;  // per-transform power-of-two scale
+    static constexpr bool kFixedChains = true;
     static constexpr int kMaxThreads = 512;
 };
 
@@ -93,6 +97,11 @@ __device__ __forceinline__ cpx<T> twid(const cpx<T> *__restrict__ tw, int e)
     return w;
 }
 
+// Shared-memory slot of logical element i: one pad slot after every 16
+// elements keeps the strided Stockham stores free of bank conflicts.
+__device__ __forceinline__ int pidx(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int padded_elems(int n) { return n + (n >> 4) + 1; }
+
 // ----------------------------------------------------------- Stockham pass
 // One radix-R pass of a self-sorting (Stockham, decimation in time) FFT on W
 // interleaved transforms of length L held in shared memory as s[n*W + w].
@@ -114,7 +123,7 @@ __device__ __forceinline__ void fft_pass(cpx<T> *s, int L, int log2W, int Ls, co
         if (task < ntask) {
             const int w = task & wmask, jj = task >> log2W;
 #pragma unroll
-            for (int r = 0; r < R; ++r) v[t][r] = s[((jj + r * LR) << log2W) + w];
+            for (int r = 0; r < R; ++r) v[t][r] = s[pidx(((jj + r * LR) << log2W) + w)];
             if (Ls > 1) {
                 const int k = jj % Ls;
 #pragma unroll
@@ -132,7 +141,7 @@ __device__ __forceinline__ void fft_pass(cpx<T> *s, int L, int log2W, int Ls, co
             const int k = jj % Ls;
             const int base = (jj - k) * R + k;  // (jj / Ls) * Ls * R + k
 #pragma unroll
-            for (int r = 0; r < R; ++r) s[((base + r * Ls) << log2W) + w] = cnorm(v[t][r]);
+            for (int r = 0; r < R; ++r) s[pidx(((base + r * Ls) << log2W) + w)] = cnorm(v[t][r]);
         }
     }
     __syncthreads();
@@ -151,10 +160,88 @@ __device__ void local_fft(cpx<T> *s, int L, int log2W, const PassPlan &pp, const
         case 2: fft_pass<T, 2, DIR>(s, L, log2W, Ls, tw, Ltab); break;
         case 3: fft_pass<T, 3, DIR>(s, L, log2W, Ls, tw, Ltab); break;
         case 5: fft_pass<T, 5, DIR>(s, L, log2W, Ls, tw, Ltab); break;
+        case 7: fft_pass<T, 7, DIR>(s, L, log2W, Ls, tw, Ltab); break;
+        case 11: fft_pass<T, 11, DIR>(s, L, log2W, Ls, tw, Ltab); break;
+        case 13: fft_pass<T, 13, DIR>(s, L, log2W, Ls, tw, Ltab); break;
         default: break;
         }
         Ls *= R;
     }
+}
+
+
+// ------------------------------------------------ compile-time pass chains
+// Power-of-two local lengths get a fixed radix chain (16, ..., 16, then the
+// remainder 2/4/8) with all index arithmetic folded at compile time, so the
+// register allocator sees straight-line code.  Twiddles come from per-pass
+// tables laid out [r-1][k] (one coalesced load per r across a warp):
+//   ptab_p[(r-1)*Ls + k] = W_{Ls*R}^{r*k},  r in [1,R), k in [0,Ls).
+template <class T, int R, int L, int W, int NT, int DIR, int Ls>
+__device__ __forceinline__ void fixed_pass(cpx<T> *s, const cpx<T> *__restrict__ tp)
+{
+    constexpr int LR = L / R;
+    constexpr int NTASK = LR * W;
+    constexpr int TPT = (NTASK + NT - 1) / NT;
+    cpx<T> v[TPT][R];
+#pragma unroll
+    for (int t = 0; t < TPT; ++t) {
+        const int task = threadIdx.x + t * NT;
+        if (NTASK % NT == 0 || task < NTASK) {
+            const int w = task % W, jj = task / W;
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[t][r] = s[pidx((jj + r * LR) * W + w)];
+            if constexpr (Ls > 1) {
+                const int k = jj % Ls;
+#pragma unroll
+                for (int r = 1; r < R; ++r) v[t][r] = cmul(v[t][r], twid<DIR>(tp, (r - 1) * Ls + k));
+            }
+            DFT<R, DIR, T>::run(v[t]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < TPT; ++t) {
+        const int task = threadIdx.x + t * NT;
+        if (NTASK % NT == 0 || task < NTASK) {
+            const int w = task % W, jj = task / W;
+            const int k = jj % Ls;
+            const int base = (jj - k) * R + k;
+#pragma unroll
+            for (int r = 0; r < R; ++r) s[pidx((base + r * Ls) * W + w)] = cnorm(v[t][r]);
+        }
+    }
+    __syncthreads();
+}
+
+__host__ __device__ constexpr int fixed_radix(int L, int Ls) { return (L / Ls) >= 16 ? 16 : L / Ls; }
+
+template <class T, int L, int W, int NT, int DIR, int Ls, int Off>
+struct FixedPasses {
+    static __device__ __forceinline__ void run(cpx<T> *s, const cpx<T> *__restrict__ ptab)
+    {
+        if constexpr (Ls < L) {
+            constexpr int R = fixed_radix(L, Ls);
+            fixed_pass<T, R, L, W, NT, DIR, Ls>(s, ptab + Off);
+            FixedPasses<T, L, W, NT, DIR, Ls * R, Off + (Ls > 1 ? Ls * (R - 1) : 0)>::run(s, ptab);
+        }
+    }
+};
+
+// threads of a fixed-length CTA: 16 elements each
+__host__ __device__ constexpr int fixed_threads(int L, int log2W)
+{
+    return ((L << log2W) / kElemsPerThread + 31) / 32 * 32 < 32 ? 32 : ((L << log2W) / kElemsPerThread + 31) / 32 * 32;
+}
+
+// Either the compile-time chain (FL > 0) or the runtime radix plan.
+template <class T, int DIR, int FL, int FW>
+__device__ __forceinline__ void run_local_fft(cpx<T> *s, int L, int log2W, const PassPlan &pp,
+                                              const cpx<T> *__restrict__ tw, int Ltab, const cpx<T> *__restrict__ ptab)
+{
+    if constexpr (FL > 0)
+        FixedPasses<T, FL, (1 << FW), fixed_threads(FL, FW), DIR, 1, 0>::run(s, ptab);
+    else
+        local_fft<T, DIR>(s, L, log2W, pp, tw, Ltab);
 }
 
 // Largest input exponent per interleaved transform w, reduced over the CTA and
@@ -195,6 +282,7 @@ struct RowArgs {
     PassPlan pp;              // local transform of length M / C
     const void *tw;           // W_{2M}^e, e in [0, 2M)
     int Ltab;                 // 2M
+    const void *ptab;         // per-pass twiddles of the compile-time chain
 };
 
 struct ColArgs {
@@ -207,7 +295,20 @@ struct ColArgs {
     PassPlan pp;              // local transform of length nx / C
     const void *tw;           // W_nx^e, e in [0, nx)
     int Ltab;                 // nx
+    const void *ptab;         // per-pass twiddles of the compile-time chain
 };
+
+// Kernel shape parameters: C = CTAs per cluster, FL = compile-time local
+// length (0: runtime plan), FW = log2 of the interleave when FL > 0.
+#define HPXFFT_SHAPE                                                                      \
+    constexpr bool kFixed = FL > 0;                                                       \
+    const int log2W = kFixed ? FW : a.log2W;                                              \
+    const int W = 1 << log2W, wmask = W - 1;                                              \
+    const int tid = threadIdx.x;                                                          \
+    const int nth = kFixed ? fixed_threads(FL, FW) : (int)blockDim.x;                     \
+    unsigned crank = 0;                                                                   \
+    if constexpr (C > 1) crank = cg::this_cluster().block_rank();                         \
+    (void)kFixed;
 
 // ------------------------------------------------------------ row r2c kernel
 // Packed-real row transform: z[m] = x[2m] + i x[2m+1], Z = DFT_M(z), then
@@ -215,7 +316,7 @@ struct ColArgs {
 //   E = (Z[k] + conj Z[M-k]) / 2,  O = (Z[k] - conj Z[M-k]) / 2.
 // Replaces the FFTW row pass core/src/shared/loop.cpp:61-69 (fft_1d_r2c_inplace,
 // loop.cpp:6-9); output row kx holds X[kx][0..M] in place of the padded input.
-template <class A, int C>
+template <class A, int C, int FL, int FW>
 __global__ void __launch_bounds__(A::kMaxThreads, 1) row_r2c_kernel(RowArgs a)
 {
     using T = typename A::T;
@@ -223,15 +324,15 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_r2c_kernel(RowArgs a)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cpx<T> *s = reinterpret_cast<cpx<T> *>(smem_raw);
     __shared__ int sE[16], sEc[16];
-    const int log2W = a.log2W, W = 1 << log2W, wmask = W - 1;
-    const int M = a.M, L = M / C;
-    unsigned crank = 0;
-    if constexpr (C > 1) crank = cg::this_cluster().block_rank();
+    HPXFFT_SHAPE
+    const int M = a.M;
+    const int L = kFixed ? FL : M / C;
+    const int nel = L << log2W;
     const int row0 = (blockIdx.x / C) * W;
     const S *in = reinterpret_cast<const S *>(a.in) + (long long)blockIdx.y * a.in_bstride;
     S *out = reinterpret_cast<S *>(a.out) + (long long)blockIdx.y * a.out_bstride;
     const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
-    const int tid = threadIdx.x, nth = blockDim.x, nel = L << log2W;
+    const cpx<T> *ptab = reinterpret_cast<const cpx<T> *>(a.ptab);
 
     if constexpr (A::kScaled) {
         if (tid < 16) sE[tid] = 0;
@@ -244,26 +345,26 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_r2c_kernel(RowArgs a)
                 const long long n = crank + (long long)C * m;
                 v = *reinterpret_cast<const double2 *>(in + row * a.in_stride + 2 * n);
             }
-            reinterpret_cast<double2 *>(s)[t] = v;
+            reinterpret_cast<double2 *>(s)[pidx(t)] = v;
             emax = max(emax, max(dbl_biased_exp(v.x), dbl_biased_exp(v.y)));
         }
         reduce_exponents<C>(emax, log2W, sE, sEc);
         for (int t = tid; t < nel; t += nth) {
-            const double2 v = reinterpret_cast<double2 *>(s)[t];
+            const double2 v = reinterpret_cast<double2 *>(s)[pidx(t)];
             const int E = scale_exp(sEc[t & wmask]);
-            s[t] = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
+            s[pidx(t)] = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
         }
     } else {
         for (int t = tid; t < nel; t += nth) {
             const int w = t & wmask, m = t >> log2W, row = row0 + w;
             cpx<T> v = czero<T>();
             if (row < a.nrows) v = load_c<A>(in + row * a.in_stride + 2 * (crank + (long long)C * m), 0);
-            s[t] = v;
+            s[pidx(t)] = v;
         }
     }
     __syncthreads();
 
-    local_fft<T, -1>(s, L, log2W, a.pp, tw, a.Ltab);
+    run_local_fft<T, -1, FL, FW>(s, L, log2W, a.pp, tw, a.Ltab, ptab);
 
     if constexpr (C == 1) {
         const int ntask = (M / 2 + 1) << log2W;
@@ -271,8 +372,8 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_r2c_kernel(RowArgs a)
             const int w = t & wmask, k = t >> log2W, row = row0 + w;
             if (row >= a.nrows) continue;
             const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
-            const cpx<T> za = s[(k << log2W) + w];
-            const cpx<T> zb = cconj(s[(((M - k) % M) << log2W) + w]);
+            const cpx<T> za = s[pidx((k << log2W) + w)];
+            const cpx<T> zb = cconj(s[pidx((((M - k) % M) << log2W) + w)]);
             const cpx<T> e = chalf(za + zb), o = chalf(za - zb);
             const cpx<T> tk = cmul(tw[k], o);
             S *orow = out + row * a.out_stride;
@@ -284,7 +385,7 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_r2c_kernel(RowArgs a)
         const int E = A::kScaled ? scale_exp(sEc[0]) : 0;
         // W_M^(c k2) = W_2M^(2 c k2)
         if (crank > 0)
-            for (int t = tid; t < L; t += nth) s[t] = cnorm(cmul(s[t], tw[2 * (int)crank * t]));
+            for (int t = tid; t < L; t += nth) s[pidx(t)] = cnorm(cmul(s[pidx(t)], tw[2 * (int)crank * t]));
         cl.sync();
         const int Lc = L / C, k20 = crank * Lc;
         constexpr int TPT = kElemsPerThread / C;
@@ -294,7 +395,7 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_r2c_kernel(RowArgs a)
             const int t = tid + u * nth;
             if (t < Lc) {
 #pragma unroll
-                for (int r = 0; r < C; ++r) v[u][r] = *cl.map_shared_rank(&s[k20 + t], r);
+                for (int r = 0; r < C; ++r) v[u][r] = *cl.map_shared_rank(&s[pidx(k20 + t)], r);
                 DFT<C, -1, T>::run(v[u]);
             }
         }
@@ -304,7 +405,7 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_r2c_kernel(RowArgs a)
             const int t = tid + u * nth;
             if (t < Lc)
 #pragma unroll
-                for (int k1 = 0; k1 < C; ++k1) s[t + Lc * k1] = cnorm(v[u][k1]);
+                for (int k1 = 0; k1 < C; ++k1) s[pidx(t + Lc * k1)] = cnorm(v[u][k1]);
         }
         cl.sync();
         // my Z[k], k = k20 + (li % Lc) + L * (li / Lc), sit at local index li
@@ -314,8 +415,8 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_r2c_kernel(RowArgs a)
             const int kp = (M - k) % M;
             const int k2p = kp % L, cp = k2p / Lc;
             const int lip = (k2p - cp * Lc) + Lc * (kp / L);
-            const cpx<T> za = s[li];
-            const cpx<T> zb = cconj(*cl.map_shared_rank(&s[lip], cp));
+            const cpx<T> za = s[pidx(li)];
+            const cpx<T> zb = cconj(*cl.map_shared_rank(&s[pidx(lip)], cp));
             const cpx<T> e = chalf(za + zb), o = chalf(za - zb);
             const cpx<T> tk = cmul(tw[k], o);
             S *orow = out + row0 * a.out_stride;
@@ -335,7 +436,7 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_r2c_kernel(RowArgs a)
 // `adjoint` the interior bins are halved first, which turns the c2r into the
 // adjoint of the r2c.  No reference counterpart (the FFTW backward direction
 // is declared in core/include/hpxfft/util/adapter_fftw.hpp:11 but unused).
-template <class A, int C>
+template <class A, int C, int FL, int FW>
 __global__ void __launch_bounds__(A::kMaxThreads, 1) row_c2r_kernel(RowArgs a)
 {
     using T = typename A::T;
@@ -343,15 +444,15 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_c2r_kernel(RowArgs a)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cpx<T> *s = reinterpret_cast<cpx<T> *>(smem_raw);
     __shared__ int sE[16], sEc[16];
-    const int log2W = a.log2W, W = 1 << log2W, wmask = W - 1;
-    const int M = a.M, L = M / C;
-    unsigned crank = 0;
-    if constexpr (C > 1) crank = cg::this_cluster().block_rank();
+    HPXFFT_SHAPE
+    const int M = a.M;
+    const int L = kFixed ? FL : M / C;
+    const int nel = L << log2W;
     const int row0 = (blockIdx.x / C) * W;
     const S *in = reinterpret_cast<const S *>(a.in) + (long long)blockIdx.y * a.in_bstride;
     S *out = reinterpret_cast<S *>(a.out) + (long long)blockIdx.y * a.out_bstride;
     const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
-    const int tid = threadIdx.x, nth = blockDim.x, nel = L << log2W;
+    const cpx<T> *ptab = reinterpret_cast<const cpx<T> *>(a.ptab);
 
     int emax = 0;
     if constexpr (A::kScaled) {
@@ -365,7 +466,7 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_c2r_kernel(RowArgs a)
                 v = *reinterpret_cast<const double2 *>(in + row * a.in_stride + 2 * (long long)k);
                 u = *reinterpret_cast<const double2 *>(in + row * a.in_stride + 2 * (long long)(M - k));
             }
-            reinterpret_cast<double2 *>(s)[t] = v;
+            reinterpret_cast<double2 *>(s)[pidx(t)] = v;
             emax = max(emax, max(max(dbl_biased_exp(v.x), dbl_biased_exp(v.y)),
                                  max(dbl_biased_exp(u.x), dbl_biased_exp(u.y))));
         }
@@ -378,7 +479,7 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_c2r_kernel(RowArgs a)
         cpx<T> xa = czero<T>(), xb = czero<T>();
         if (row < a.nrows) {
             if constexpr (A::kScaled) {
-                const double2 v = reinterpret_cast<double2 *>(s)[t];
+                const double2 v = reinterpret_cast<double2 *>(s)[pidx(t)];
                 xa = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
             } else {
                 xa = load_c<A>(in + row * a.in_stride + 2 * (long long)k, 0);
@@ -394,18 +495,18 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_c2r_kernel(RowArgs a)
         }
         const cpx<T> xbc = cconj(xb);
         const cpx<T> sum = xa + xbc, dif = xa - xbc;
-        s[t] = cnorm(sum + mul_i<+1>(cmul(twid<+1>(tw, k), dif)));
+        s[pidx(t)] = cnorm(sum + mul_i<+1>(cmul(twid<+1>(tw, k), dif)));
     }
     __syncthreads();
 
-    local_fft<T, +1>(s, L, log2W, a.pp, tw, a.Ltab);
+    run_local_fft<T, +1, FL, FW>(s, L, log2W, a.pp, tw, a.Ltab, ptab);
 
     if constexpr (C == 1) {
         for (int t = tid; t < nel; t += nth) {
             const int w = t & wmask, m = t >> log2W, row = row0 + w;
             if (row >= a.nrows) continue;
             const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
-            store_c<A>(out + row * a.out_stride + 2 * (long long)m, s[t], E);
+            store_c<A>(out + row * a.out_stride + 2 * (long long)m, s[pidx(t)], E);
             if (m == 0) {
                 out[row * a.out_stride + 2 * (long long)M] = (S)0;
                 out[row * a.out_stride + 2 * (long long)M + 1] = (S)0;
@@ -415,13 +516,14 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_c2r_kernel(RowArgs a)
         cg::cluster_group cl = cg::this_cluster();
         const int E = A::kScaled ? scale_exp(sEc[0]) : 0;
         if (crank > 0)
-            for (int t = tid; t < L; t += nth) s[t] = cnorm(cmul(s[t], twid<+1>(tw, 2 * (int)crank * t)));
+            for (int t = tid; t < L; t += nth)
+                s[pidx(t)] = cnorm(cmul(s[pidx(t)], twid<+1>(tw, 2 * (int)crank * t)));
         cl.sync();
         const int Lc = L / C, k20 = crank * Lc;
         for (int t = tid; t < Lc; t += nth) {
             cpx<T> v[C];
 #pragma unroll
-            for (int r = 0; r < C; ++r) v[r] = *cl.map_shared_rank(&s[k20 + t], r);
+            for (int r = 0; r < C; ++r) v[r] = *cl.map_shared_rank(&s[pidx(k20 + t)], r);
             DFT<C, +1, T>::run(v);
             if (row0 < a.nrows)
 #pragma unroll
@@ -440,7 +542,7 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_c2r_kernel(RowArgs a)
 // In-place length-nx c2c on strips of W adjacent columns of the [kx][ky]
 // array.  Replaces transpose -> FFTW c2c -> transpose back
 // (core/src/shared/loop.cpp:72-102, fft_1d_c2c_inplace loop.cpp:11-15).
-template <class A, int C, int DIR>
+template <class A, int C, int DIR, int FL, int FW>
 __global__ void __launch_bounds__(A::kMaxThreads, 1) col_kernel(ColArgs a)
 {
     using T = typename A::T;
@@ -448,14 +550,13 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) col_kernel(ColArgs a)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cpx<T> *s = reinterpret_cast<cpx<T> *>(smem_raw);
     __shared__ int sE[16], sEc[16];
-    const int log2W = a.log2W, W = 1 << log2W, wmask = W - 1;
-    const int L = a.nx / C;
-    unsigned crank = 0;
-    if constexpr (C > 1) crank = cg::this_cluster().block_rank();
+    HPXFFT_SHAPE
+    const int L = kFixed ? FL : a.nx / C;
+    const int nel = L << log2W;
     const int col0 = (blockIdx.x / C) * W;
     S *data = reinterpret_cast<S *>(a.data) + (long long)blockIdx.y * a.bstride;
     const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
-    const int tid = threadIdx.x, nth = blockDim.x, nel = L << log2W;
+    const cpx<T> *ptab = reinterpret_cast<const cpx<T> *>(a.ptab);
 
     if constexpr (A::kScaled) {
         if (tid < 16) sE[tid] = 0;
@@ -468,14 +569,14 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) col_kernel(ColArgs a)
                 const long long n = crank + (long long)C * m;
                 v = *reinterpret_cast<const double2 *>(data + n * a.row_stride + 2 * (long long)col);
             }
-            reinterpret_cast<double2 *>(s)[t] = v;
+            reinterpret_cast<double2 *>(s)[pidx(t)] = v;
             emax = max(emax, max(dbl_biased_exp(v.x), dbl_biased_exp(v.y)));
         }
         reduce_exponents<C>(emax, log2W, sE, sEc);
         for (int t = tid; t < nel; t += nth) {
-            const double2 v = reinterpret_cast<double2 *>(s)[t];
+            const double2 v = reinterpret_cast<double2 *>(s)[pidx(t)];
             const int E = scale_exp(sEc[t & wmask]);
-            s[t] = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
+            s[pidx(t)] = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
         }
     } else {
         for (int t = tid; t < nel; t += nth) {
@@ -483,26 +584,26 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) col_kernel(ColArgs a)
             cpx<T> v = czero<T>();
             if (col < a.ncols)
                 v = load_c<A>(data + (crank + (long long)C * m) * a.row_stride + 2 * (long long)col, 0);
-            s[t] = v;
+            s[pidx(t)] = v;
         }
     }
     __syncthreads();
 
-    local_fft<T, DIR>(s, L, log2W, a.pp, tw, a.Ltab);
+    run_local_fft<T, DIR, FL, FW>(s, L, log2W, a.pp, tw, a.Ltab, ptab);
 
     if constexpr (C == 1) {
         for (int t = tid; t < nel; t += nth) {
             const int w = t & wmask, k = t >> log2W, col = col0 + w;
             if (col >= a.ncols) continue;
             const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
-            store_c<A>(data + (long long)k * a.row_stride + 2 * (long long)col, s[t], E);
+            store_c<A>(data + (long long)k * a.row_stride + 2 * (long long)col, s[pidx(t)], E);
         }
     } else {
         cg::cluster_group cl = cg::this_cluster();
         if (crank > 0)
             for (int t = tid; t < nel; t += nth) {
                 const int k2 = t >> log2W;
-                s[t] = cnorm(cmul(s[t], twid<DIR>(tw, (int)crank * k2)));
+                s[pidx(t)] = cnorm(cmul(s[pidx(t)], twid<DIR>(tw, (int)crank * k2)));
             }
         cl.sync();
         const int Lc = L / C, k20 = crank * Lc;
@@ -511,7 +612,7 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) col_kernel(ColArgs a)
             const int w = t & wmask, k2 = k20 + (t >> log2W), col = col0 + w;
             cpx<T> v[C];
 #pragma unroll
-            for (int r = 0; r < C; ++r) v[r] = *cl.map_shared_rank(&s[(k2 << log2W) + w], r);
+            for (int r = 0; r < C; ++r) v[r] = *cl.map_shared_rank(&s[pidx((k2 << log2W) + w)], r);
             DFT<C, DIR, T>::run(v);
             if (col < a.ncols) {
                 const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
@@ -544,6 +645,28 @@ __global__ void twiddle_kernel(cpx<T> *tab, int N)
         tab[e] = cpx<ff>{r, i};
     } else {
         tab[e] = cpx<T>{(T)re, (T)im};
+    }
+}
+
+// Per-pass table of a compile-time chain: out[(r-1)*Ls + k] = W_{Ls R}^{r k}.
+template <class T>
+__global__ void pass_twiddle_kernel(cpx<T> *out, int Ls, int R)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= Ls * (R - 1)) return;
+    const int r = 1 + e / Ls, k = e % Ls;
+    double sn, cs;
+    sincospi(2.0 * (double)(r * k) / (double)(Ls * R), &sn, &cs);
+    const double re = cs, im = -sn;
+    if constexpr (std::is_same<T, ff>::value) {
+        ff a, b;
+        a.hi = (float)re;
+        a.lo = (float)(re - (double)a.hi);
+        b.hi = (float)im;
+        b.lo = (float)(im - (double)b.hi);
+        out[e] = cpx<ff>{a, b};
+    } else {
+        out[e] = cpx<T>{(T)re, (T)im};
     }
 }
 

@@ -1,6 +1,6 @@
-// Launchers for the transform kernels of one compute type.  Each
-// kernels_<type>.cu instantiates them for its type, so the three compute
-// types compile in parallel.
+// Launchers for the transform kernels of one compute type.  Row kernels,
+// column kernels and twiddle generators are defined in separate translation
+// units (kernels_<type>_{rows,cols}.cu) so they compile in parallel.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -15,17 +15,37 @@ struct LaunchShape {
     int cluster;
 };
 
+// Compile-time configurations (local length L, log2 interleave, cluster size).
+// Rows: L >= 4096 one row per CTA, shorter rows packed up to 4096 elements.
+#define HPXFFT_ROW_FIXED_COMMON(X) X(8192, 0, 1) X(8192, 0, 2) X(4096, 0, 1) X(2048, 1, 1) X(1024, 2, 1) X(512, 3, 1) X(256, 4, 1)
+#define HPXFFT_ROW_FIXED_F32(X) X(16384, 0, 1)
+// Columns: power-of-two nx >= 2048 always splits into local length 2048.
+#define HPXFFT_COL_FIXED(X, LW) X(2048, LW, 1) X(2048, LW, 2) X(2048, LW, 4) X(2048, LW, 8) X(2048, LW, 16)
+
 template <class A>
-struct Launch {
-    // Raise the dynamic shared memory limit and allow 16-CTA clusters.
+struct RowLaunch {
     static cudaError_t prepare();
-    static cudaError_t row_r2c(const RowArgs &a, const LaunchShape &s, cudaStream_t st);
-    static cudaError_t row_c2r(const RowArgs &a, const LaunchShape &s, cudaStream_t st);
-    static cudaError_t col(const ColArgs &a, int dir, const LaunchShape &s, cudaStream_t st);
-    static cudaError_t twiddles(void *tab, int n, cudaStream_t st);
+    static bool has_fixed(int L, int log2W, int C);
+    // FL = 0 selects the runtime radix plan
+    static cudaError_t r2c(const RowArgs &a, const LaunchShape &s, int FL, cudaStream_t st);
+    static cudaError_t c2r(const RowArgs &a, const LaunchShape &s, int FL, cudaStream_t st);
 };
 
-#ifdef HPXFFT_DEFINE_LAUNCHERS
+template <class A>
+struct ColLaunch {
+    static constexpr int kLog2W = sizeof(typename A::S) == 4 ? 3 : 2;  // 64-byte row segments
+    static cudaError_t prepare();
+    static bool has_fixed(int L, int log2W, int C);
+    static cudaError_t run(const ColArgs &a, int dir, const LaunchShape &s, int FL, cudaStream_t st);
+};
+
+template <class A>
+struct TwiddleLaunch {
+    static cudaError_t full(void *tab, int n, cudaStream_t st);
+    static cudaError_t pass(void *tab, int Ls, int R, cudaStream_t st);
+};
+
+#if defined(HPXFFT_DEFINE_ROWS) || defined(HPXFFT_DEFINE_COLS) || defined(HPXFFT_DEFINE_TWIDDLES)
 template <class K, class Args>
 static cudaError_t launch_cluster(K kernel, const Args &a, const LaunchShape &s, cudaStream_t st)
 {
@@ -47,92 +67,167 @@ static cudaError_t launch_cluster(K kernel, const Args &a, const LaunchShape &s,
 template <class K>
 static cudaError_t set_attrs(K kernel, bool nonportable)
 {
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     if (e != cudaSuccess) return e;
     if (nonportable) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     return e;
 }
-
-template <class A>
-cudaError_t Launch<A>::prepare()
-{
-    cudaError_t e = cudaSuccess;
-#define HPXFFT_TRY(x)                 \
-    do {                              \
-        e = (x);                      \
-        if (e != cudaSuccess) return e; \
+#define HPXFFT_TRY(x)                   \
+    do {                                \
+        cudaError_t e_ = (x);           \
+        if (e_ != cudaSuccess) return e_; \
     } while (0)
-    HPXFFT_TRY(set_attrs(row_r2c_kernel<A, 1>, false));
-    HPXFFT_TRY(set_attrs(row_r2c_kernel<A, 2>, false));
-    HPXFFT_TRY(set_attrs(row_r2c_kernel<A, 4>, false));
-    HPXFFT_TRY(set_attrs(row_c2r_kernel<A, 1>, false));
-    HPXFFT_TRY(set_attrs(row_c2r_kernel<A, 2>, false));
-    HPXFFT_TRY(set_attrs(row_c2r_kernel<A, 4>, false));
-    HPXFFT_TRY(set_attrs(col_kernel<A, 1, -1>, false));
-    HPXFFT_TRY(set_attrs(col_kernel<A, 2, -1>, false));
-    HPXFFT_TRY(set_attrs(col_kernel<A, 4, -1>, false));
-    HPXFFT_TRY(set_attrs(col_kernel<A, 8, -1>, false));
-    HPXFFT_TRY(set_attrs(col_kernel<A, 16, -1>, true));
-    HPXFFT_TRY(set_attrs(col_kernel<A, 1, +1>, false));
-    HPXFFT_TRY(set_attrs(col_kernel<A, 2, +1>, false));
-    HPXFFT_TRY(set_attrs(col_kernel<A, 4, +1>, false));
-    HPXFFT_TRY(set_attrs(col_kernel<A, 8, +1>, false));
-    HPXFFT_TRY(set_attrs(col_kernel<A, 16, +1>, true));
-#undef HPXFFT_TRY
-    return e;
-}
+#endif
 
+#ifdef HPXFFT_DEFINE_ROWS
 template <class A>
-cudaError_t Launch<A>::row_r2c(const RowArgs &a, const LaunchShape &s, cudaStream_t st)
+cudaError_t RowLaunch<A>::prepare()
 {
-    switch (s.cluster) {
-    case 1: return launch_cluster(row_r2c_kernel<A, 1>, a, s, st);
-    case 2: return launch_cluster(row_r2c_kernel<A, 2>, a, s, st);
-    case 4: return launch_cluster(row_r2c_kernel<A, 4>, a, s, st);
-    default: return cudaErrorInvalidValue;
+    HPXFFT_TRY(set_attrs(row_r2c_kernel<A, 1, 0, 0>, false));
+    HPXFFT_TRY(set_attrs(row_r2c_kernel<A, 2, 0, 0>, false));
+    HPXFFT_TRY(set_attrs(row_r2c_kernel<A, 4, 0, 0>, false));
+    HPXFFT_TRY(set_attrs(row_c2r_kernel<A, 1, 0, 0>, false));
+    HPXFFT_TRY(set_attrs(row_c2r_kernel<A, 2, 0, 0>, false));
+    HPXFFT_TRY(set_attrs(row_c2r_kernel<A, 4, 0, 0>, false));
+    if constexpr (A::kFixedChains) {
+#define HPXFFT_X(L, W, C)                                                  \
+    HPXFFT_TRY(set_attrs(row_r2c_kernel<A, C, L, W>, false));              \
+    HPXFFT_TRY(set_attrs(row_c2r_kernel<A, C, L, W>, false));
+        HPXFFT_ROW_FIXED_COMMON(HPXFFT_X)
+        if constexpr (sizeof(typename A::S) == 4) { HPXFFT_ROW_FIXED_F32(HPXFFT_X) }
+#undef HPXFFT_X
     }
+    return cudaSuccess;
 }
 
 template <class A>
-cudaError_t Launch<A>::row_c2r(const RowArgs &a, const LaunchShape &s, cudaStream_t st)
+bool RowLaunch<A>::has_fixed(int L, int log2W, int C)
 {
-    switch (s.cluster) {
-    case 1: return launch_cluster(row_c2r_kernel<A, 1>, a, s, st);
-    case 2: return launch_cluster(row_c2r_kernel<A, 2>, a, s, st);
-    case 4: return launch_cluster(row_c2r_kernel<A, 4>, a, s, st);
-    default: return cudaErrorInvalidValue;
-    }
+    if constexpr (!A::kFixedChains) return false;
+#define HPXFFT_X(L_, W_, C_) \
+    if (L == L_ && log2W == W_ && C == C_) return true;
+    HPXFFT_ROW_FIXED_COMMON(HPXFFT_X)
+    if constexpr (sizeof(typename A::S) == 4) { HPXFFT_ROW_FIXED_F32(HPXFFT_X) }
+#undef HPXFFT_X
+    return false;
 }
 
 template <class A>
-cudaError_t Launch<A>::col(const ColArgs &a, int dir, const LaunchShape &s, cudaStream_t st)
+cudaError_t RowLaunch<A>::r2c(const RowArgs &a, const LaunchShape &s, int FL, cudaStream_t st)
 {
-    if (dir < 0) {
-        switch (s.cluster) {
-        case 1: return launch_cluster(col_kernel<A, 1, -1>, a, s, st);
-        case 2: return launch_cluster(col_kernel<A, 2, -1>, a, s, st);
-        case 4: return launch_cluster(col_kernel<A, 4, -1>, a, s, st);
-        case 8: return launch_cluster(col_kernel<A, 8, -1>, a, s, st);
-        case 16: return launch_cluster(col_kernel<A, 16, -1>, a, s, st);
-        default: return cudaErrorInvalidValue;
+    if constexpr (A::kFixedChains) {
+        if (FL) {
+#define HPXFFT_X(L_, W_, C_) \
+    if (FL == L_ && a.log2W == W_ && s.cluster == C_) return launch_cluster(row_r2c_kernel<A, C_, L_, W_>, a, s, st);
+            HPXFFT_ROW_FIXED_COMMON(HPXFFT_X)
+            if constexpr (sizeof(typename A::S) == 4) { HPXFFT_ROW_FIXED_F32(HPXFFT_X) }
+#undef HPXFFT_X
+            return cudaErrorInvalidValue;
         }
     }
     switch (s.cluster) {
-    case 1: return launch_cluster(col_kernel<A, 1, +1>, a, s, st);
-    case 2: return launch_cluster(col_kernel<A, 2, +1>, a, s, st);
-    case 4: return launch_cluster(col_kernel<A, 4, +1>, a, s, st);
-    case 8: return launch_cluster(col_kernel<A, 8, +1>, a, s, st);
-    case 16: return launch_cluster(col_kernel<A, 16, +1>, a, s, st);
+    case 1: return launch_cluster(row_r2c_kernel<A, 1, 0, 0>, a, s, st);
+    case 2: return launch_cluster(row_r2c_kernel<A, 2, 0, 0>, a, s, st);
+    case 4: return launch_cluster(row_r2c_kernel<A, 4, 0, 0>, a, s, st);
     default: return cudaErrorInvalidValue;
     }
 }
 
 template <class A>
-cudaError_t Launch<A>::twiddles(void *tab, int n, cudaStream_t st)
+cudaError_t RowLaunch<A>::c2r(const RowArgs &a, const LaunchShape &s, int FL, cudaStream_t st)
+{
+    if constexpr (A::kFixedChains) {
+        if (FL) {
+#define HPXFFT_X(L_, W_, C_) \
+    if (FL == L_ && a.log2W == W_ && s.cluster == C_) return launch_cluster(row_c2r_kernel<A, C_, L_, W_>, a, s, st);
+            HPXFFT_ROW_FIXED_COMMON(HPXFFT_X)
+            if constexpr (sizeof(typename A::S) == 4) { HPXFFT_ROW_FIXED_F32(HPXFFT_X) }
+#undef HPXFFT_X
+            return cudaErrorInvalidValue;
+        }
+    }
+    switch (s.cluster) {
+    case 1: return launch_cluster(row_c2r_kernel<A, 1, 0, 0>, a, s, st);
+    case 2: return launch_cluster(row_c2r_kernel<A, 2, 0, 0>, a, s, st);
+    case 4: return launch_cluster(row_c2r_kernel<A, 4, 0, 0>, a, s, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+#endif
+
+#ifdef HPXFFT_DEFINE_COLS
+template <class A>
+cudaError_t ColLaunch<A>::prepare()
+{
+#define HPXFFT_G(C, NP)                                           \
+    HPXFFT_TRY(set_attrs(col_kernel<A, C, -1, 0, 0>, NP));        \
+    HPXFFT_TRY(set_attrs(col_kernel<A, C, +1, 0, 0>, NP));
+    HPXFFT_G(1, false) HPXFFT_G(2, false) HPXFFT_G(4, false) HPXFFT_G(8, false) HPXFFT_G(16, true)
+#undef HPXFFT_G
+    if constexpr (A::kFixedChains) {
+#define HPXFFT_X(L, W, C)                                                 \
+    HPXFFT_TRY(set_attrs(col_kernel<A, C, -1, L, W>, C > 8));             \
+    HPXFFT_TRY(set_attrs(col_kernel<A, C, +1, L, W>, C > 8));
+        HPXFFT_COL_FIXED(HPXFFT_X, kLog2W)
+#undef HPXFFT_X
+    }
+    return cudaSuccess;
+}
+
+template <class A>
+bool ColLaunch<A>::has_fixed(int L, int log2W, int C)
+{
+    if constexpr (!A::kFixedChains) return false;
+#define HPXFFT_X(L_, W_, C_) \
+    if (L == L_ && log2W == W_ && C == C_) return true;
+    HPXFFT_COL_FIXED(HPXFFT_X, kLog2W)
+#undef HPXFFT_X
+    return false;
+}
+
+template <class A>
+cudaError_t ColLaunch<A>::run(const ColArgs &a, int dir, const LaunchShape &s, int FL, cudaStream_t st)
+{
+    if constexpr (A::kFixedChains) {
+        if (FL) {
+#define HPXFFT_X(L_, W_, C_)                                                              \
+    if (FL == L_ && a.log2W == W_ && s.cluster == C_)                                     \
+        return dir < 0 ? launch_cluster(col_kernel<A, C_, -1, L_, W_>, a, s, st)          \
+                       : launch_cluster(col_kernel<A, C_, +1, L_, W_>, a, s, st);
+            HPXFFT_COL_FIXED(HPXFFT_X, kLog2W)
+#undef HPXFFT_X
+            return cudaErrorInvalidValue;
+        }
+    }
+#define HPXFFT_G(C_)                                                                       \
+    case C_:                                                                               \
+        return dir < 0 ? launch_cluster(col_kernel<A, C_, -1, 0, 0>, a, s, st)            \
+                       : launch_cluster(col_kernel<A, C_, +1, 0, 0>, a, s, st);
+    switch (s.cluster) {
+        HPXFFT_G(1) HPXFFT_G(2) HPXFFT_G(4) HPXFFT_G(8) HPXFFT_G(16)
+    default: return cudaErrorInvalidValue;
+    }
+#undef HPXFFT_G
+}
+#endif
+
+#ifdef HPXFFT_DEFINE_TWIDDLES
+template <class A>
+cudaError_t TwiddleLaunch<A>::full(void *tab, int n, cudaStream_t st)
 {
     using T = typename A::T;
     const int threads = 256;
     twiddle_kernel<T><<<(n + threads - 1) / threads, threads, 0, st>>>(reinterpret_cast<cpx<T> *>(tab), n);
+    return cudaGetLastError();
+}
+
+template <class A>
+cudaError_t TwiddleLaunch<A>::pass(void *tab, int Ls, int R, cudaStream_t st)
+{
+    using T = typename A::T;
+    const int n = Ls * (R - 1), threads = 256;
+    if (n <= 0) return cudaSuccess;
+    pass_twiddle_kernel<T><<<(n + threads - 1) / threads, threads, 0, st>>>(reinterpret_cast<cpx<T> *>(tab), Ls, R);
     return cudaGetLastError();
 }
 #endif

@@ -39,6 +39,8 @@ struct DimPlan {
     int C = 1;
     int log2W = 0;
     int L = 0;
+    int FL = 0;              // L when a compile-time pass chain is used, else 0
+    void *ptab = nullptr;    // per-pass twiddles of that chain
 };
 
 }  // namespace hpxfft_gpu
@@ -69,23 +71,22 @@ struct hpxfft_plan_s {
 namespace hpxfft_gpu {
 
 // radix sequence for a local length L: 16s first, then the power-of-two
-// remainder, then 3s and 5s
+// remainder, then the odd primes 3, 5, 7, 11, 13
 static bool factorize(int L, int max_radix, PassPlan &pp)
 {
     pp.n = 0;
     int rest = L;
-    int p3 = 0, p5 = 0;
-    while (rest % 3 == 0) rest /= 3, ++p3;
-    while (rest % 5 == 0) rest /= 5, ++p5;
-    if (rest & (rest - 1)) return false;  // a factor other than 2, 3, 5
+    std::vector<int> odd;
+    for (int q : {3, 5, 7, 11, 13})
+        while (rest % q == 0) rest /= q, odd.push_back(q);
+    if (rest & (rest - 1)) return false;  // a prime factor above 13
     int p2 = 0;
     while ((1 << p2) < rest) ++p2;
     const int lmax = max_radix == 16 ? 4 : 3;
     std::vector<int> r;
     while (p2 >= lmax) r.push_back(1 << lmax), p2 -= lmax;
     if (p2 > 0) r.push_back(1 << p2);
-    for (int i = 0; i < p3; ++i) r.push_back(3);
-    for (int i = 0; i < p5; ++i) r.push_back(5);
+    for (int q : odd) r.push_back(q);
     if ((int)r.size() > kMaxPasses) return false;
     pp.n = (int)r.size();
     for (size_t i = 0; i < r.size(); ++i) pp.radix[i] = r[i];
@@ -122,7 +123,7 @@ static bool plan_rows(hpxfft_plan_s &p)
         d.pp = pp;
         const int nel = L << log2W;
         d.shape.threads = threads_for(nel);
-        d.shape.smem = (size_t)nel * cbytes;
+        d.shape.smem = (size_t)padded_elems(nel) * cbytes;
         d.shape.cluster = C;
         const size_t groups = (p.nx + ((size_t)1 << log2W) - 1) >> log2W;
         d.shape.grid = dim3((unsigned)(groups * C), (unsigned)p.batch, 1);
@@ -151,7 +152,7 @@ static bool plan_cols(hpxfft_plan_s &p)
         d.pp = pp;
         const int nel = L << log2W;
         d.shape.threads = threads_for(nel);
-        d.shape.smem = (size_t)nel * cbytes;
+        d.shape.smem = (size_t)padded_elems(nel) * cbytes;
         d.shape.cluster = C;
         const size_t strips = (p.dcy + ((size_t)1 << log2W) - 1) >> log2W;
         d.shape.grid = dim3((unsigned)(strips * C), (unsigned)p.batch, 1);
@@ -163,8 +164,35 @@ static bool plan_cols(hpxfft_plan_s &p)
 template <class A>
 static cudaError_t prepare_once()
 {
-    static cudaError_t status = Launch<A>::prepare();
+    static cudaError_t status = []() {
+        cudaError_t e = RowLaunch<A>::prepare();
+        return e != cudaSuccess ? e : ColLaunch<A>::prepare();
+    }();
     return status;
+}
+
+static bool has_fixed(int prec, bool rows, const DimPlan &d)
+{
+    switch (prec) {
+    case HPXFFT_PREC_F64:
+        return rows ? RowLaunch<ArithFF>::has_fixed(d.L, d.log2W, d.C) : ColLaunch<ArithFF>::has_fixed(d.L, d.log2W, d.C);
+    case HPXFFT_PREC_F32:
+        return rows ? RowLaunch<ArithF32>::has_fixed(d.L, d.log2W, d.C)
+                    : ColLaunch<ArithF32>::has_fixed(d.L, d.log2W, d.C);
+    default: return false;
+    }
+}
+
+// (Ls, R) of every pass of the compile-time chain for length L, in order
+static std::vector<std::pair<int, int>> fixed_chain(int L)
+{
+    std::vector<std::pair<int, int>> v;
+    for (int Ls = 1; Ls < L;) {
+        const int R = (L / Ls) >= 16 ? 16 : L / Ls;
+        v.push_back({Ls, R});
+        Ls *= R;
+    }
+    return v;
 }
 
 static cudaError_t prepare_prec(int prec)
@@ -179,10 +207,43 @@ static cudaError_t prepare_prec(int prec)
 static cudaError_t gen_twiddles(int prec, void *tab, int n, cudaStream_t st)
 {
     switch (prec) {
-    case HPXFFT_PREC_F64: return Launch<ArithFF>::twiddles(tab, n, st);
-    case HPXFFT_PREC_F64_NATIVE: return Launch<ArithF64>::twiddles(tab, n, st);
-    default: return Launch<ArithF32>::twiddles(tab, n, st);
+    case HPXFFT_PREC_F64: return TwiddleLaunch<ArithFF>::full(tab, n, st);
+    case HPXFFT_PREC_F64_NATIVE: return TwiddleLaunch<ArithF64>::full(tab, n, st);
+    default: return TwiddleLaunch<ArithF32>::full(tab, n, st);
     }
+}
+
+static cudaError_t gen_pass_twiddles(int prec, void *tab, int Ls, int R, cudaStream_t st)
+{
+    switch (prec) {
+    case HPXFFT_PREC_F64: return TwiddleLaunch<ArithFF>::pass(tab, Ls, R, st);
+    case HPXFFT_PREC_F64_NATIVE: return TwiddleLaunch<ArithF64>::pass(tab, Ls, R, st);
+    default: return TwiddleLaunch<ArithF32>::pass(tab, Ls, R, st);
+    }
+}
+
+// Allocate and fill the per-pass tables when the dimension uses a fixed chain.
+static int setup_fixed(hpxfft_plan_s &p, DimPlan &d, bool rows, cudaStream_t st)
+{
+    d.FL = 0;
+    if (!has_fixed(p.prec, rows, d)) return HPXFFT_OK;
+    const auto chain = fixed_chain(d.L);
+    size_t entries = 0;
+    for (auto &c : chain)
+        if (c.first > 1) entries += (size_t)c.first * (c.second - 1);
+    if (cudaMalloc(&d.ptab, p.tw_elem * (entries ? entries : 1)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(HPXFFT_ERR_ALLOC, "pass twiddle table");
+    }
+    size_t off = 0;
+    for (auto &c : chain) {
+        if (c.first == 1) continue;
+        cudaError_t e = gen_pass_twiddles(p.prec, (char *)d.ptab + off * p.tw_elem, c.first, c.second, st);
+        if (e != cudaSuccess) return cuda_fail(e, "pass twiddle generation");
+        off += (size_t)c.first * (c.second - 1);
+    }
+    d.FL = d.L;
+    return HPXFFT_OK;
 }
 
 static RowArgs row_args(const hpxfft_plan_s &p, const void *in, void *out, int adjoint)
@@ -201,6 +262,7 @@ static RowArgs row_args(const hpxfft_plan_s &p, const void *in, void *out, int a
     a.pp = p.row.pp;
     a.tw = p.tw_row;
     a.Ltab = (int)(2 * p.M);
+    a.ptab = p.row.ptab;
     return a;
 }
 
@@ -216,6 +278,7 @@ static ColArgs col_args(const hpxfft_plan_s &p, void *data)
     a.pp = p.col.pp;
     a.tw = p.tw_col;
     a.Ltab = (int)p.nx;
+    a.ptab = p.col.ptab;
     return a;
 }
 
@@ -239,9 +302,9 @@ static cudaError_t run_forward(hpxfft_plan_s &p, const void *in, void *out)
     cudaError_t e;
     cudaEvent_t *ev = next_slot(p);
     if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
-    if ((e = Launch<A>::row_r2c(row_args(p, in, out, 0), p.row.shape, p.stream)) != cudaSuccess) return e;
+    if ((e = RowLaunch<A>::r2c(row_args(p, in, out, 0), p.row.shape, p.row.FL, p.stream)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
-    if ((e = Launch<A>::col(col_args(p, out), -1, p.col.shape, p.stream)) != cudaSuccess) return e;
+    if ((e = ColLaunch<A>::run(col_args(p, out), -1, p.col.shape, p.col.FL, p.stream)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[2], p.stream)) != cudaSuccess) return e;
     ++p.next;
     return cudaSuccess;
@@ -253,9 +316,9 @@ static cudaError_t run_inverse(hpxfft_plan_s &p, void *data, int adjoint)
     cudaError_t e;
     cudaEvent_t *ev = next_slot(p);
     if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
-    if ((e = Launch<A>::col(col_args(p, data), +1, p.col.shape, p.stream)) != cudaSuccess) return e;
+    if ((e = ColLaunch<A>::run(col_args(p, data), +1, p.col.shape, p.col.FL, p.stream)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
-    if ((e = Launch<A>::row_c2r(row_args(p, data, data, adjoint), p.row.shape, p.stream)) != cudaSuccess)
+    if ((e = RowLaunch<A>::c2r(row_args(p, data, data, adjoint), p.row.shape, p.row.FL, p.stream)) != cudaSuccess)
         return e;
     if ((e = cudaEventRecord(ev[2], p.stream)) != cudaSuccess) return e;
     ++p.next;
@@ -332,10 +395,10 @@ static std::string describe(const hpxfft_plan_s &p, const DimPlan &d, const char
     for (int i = 0; i < d.pp.n; ++i) radices += (i ? "x" : "") + std::to_string(d.pp.radix[i]);
     if (radices.empty()) radices = "1";
     snprintf(buf, sizeof(buf),
-             "(gpu-%s n=%zu cluster=%d local=%d radices=%s interleaved=%d grid=%ux%u threads=%d smem=%zu "
+             "(gpu-%s n=%zu cluster=%d local=%d radices=%s chain=%s interleaved=%d grid=%ux%u threads=%d smem=%zu "
              "precision=%s)",
-             what, len, d.C, d.L, radices.c_str(), 1 << d.log2W, d.shape.grid.x, d.shape.grid.y, d.shape.threads,
-             d.shape.smem,
+             what, len, d.C, d.L, radices.c_str(), d.FL ? "compile-time" : "runtime", 1 << d.log2W, d.shape.grid.x,
+             d.shape.grid.y, d.shape.threads, d.shape.smem,
              p.prec == HPXFFT_PREC_F64 ? "f64-floatfloat" : (p.prec == HPXFFT_PREC_F64_NATIVE ? "f64-dfma" : "f32"));
     return buf;
 }
@@ -393,7 +456,7 @@ int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
     if (!plan_rows(*p) || !plan_cols(*p)) {
         delete p;
         return fail(HPXFFT_ERR_UNSUPPORTED_SIZE,
-                    "sizes must factor into 2, 3 and 5 and fit the per-cluster shared memory");
+                    "sizes must have no prime factor above 13 and fit the per-cluster shared memory");
     }
     cudaError_t e = prepare_prec(precision);
     if (e != cudaSuccess) {
@@ -421,6 +484,13 @@ int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
         hpxfft_plan_destroy(p);
         return fail(HPXFFT_ERR_ALLOC, "twiddle tables");
     }
+    int rc = setup_fixed(*p, p->row, true, p->stream);
+    if (rc == HPXFFT_OK) rc = setup_fixed(*p, p->col, false, p->stream);
+    if (rc != HPXFFT_OK) {
+        std::string msg = g_last_error;
+        hpxfft_plan_destroy(p);
+        return fail(rc, msg);
+    }
     if ((e = gen_twiddles(precision, p->tw_row, (int)(2 * p->M), p->stream)) != cudaSuccess ||
         (e = gen_twiddles(precision, p->tw_col, (int)p->nx, p->stream)) != cudaSuccess ||
         (e = cudaStreamSynchronize(p->stream)) != cudaSuccess) {
@@ -445,6 +515,8 @@ int hpxfft_plan_destroy(hpxfft_plan p)
     if (p->stream) cudaStreamSynchronize(p->stream);
     cudaFree(p->tw_row);
     cudaFree(p->tw_col);
+    cudaFree(p->row.ptab);
+    cudaFree(p->col.ptab);
     cudaFree(p->dbuf);
     for (auto &slot : p->kev)
         for (auto &ev : slot)
@@ -459,7 +531,14 @@ int hpxfft_plan_destroy(hpxfft_plan p)
 int hpxfft_plan_set_stream(hpxfft_plan p, void *stream)
 {
     if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
-    p->stream = stream ? (cudaStream_t)stream : p->own_stream;
+    p->stream = (cudaStream_t)stream;  // verbatim: NULL is the legacy default stream
+    return HPXFFT_OK;
+}
+
+int hpxfft_plan_get_stream(hpxfft_plan p, void **stream)
+{
+    if (!p || !stream) return fail(HPXFFT_ERR_INVALID_ARG, "null argument");
+    *stream = (void *)p->stream;
     return HPXFFT_OK;
 }
 

@@ -33,6 +33,7 @@ SIGNATURES = {
     "hpxfft_plan_create": (_ci, [ctypes.POINTER(_vp), _sz, _sz, _sz, _ci, _cs]),
     "hpxfft_plan_destroy": (_ci, [_vp]),
     "hpxfft_plan_set_stream": (_ci, [_vp, _vp]),
+    "hpxfft_plan_get_stream": (_ci, [_vp, ctypes.POINTER(_vp)]),
     "hpxfft_plan_buffer_bytes": (_ci, [_vp, ctypes.POINTER(_sz)]),
     "hpxfft_execute_r2c": (_ci, [_vp, _vp]),
     "hpxfft_execute_r2c_oop": (_ci, [_vp, _vp, _vp]),

@@ -41,6 +41,9 @@ class Plan:
         self._h = ctypes.c_void_p()
         flag = plan_flag.encode() if isinstance(plan_flag, str) else plan_flag
         _capi.check(lib.hpxfft_plan_create(ctypes.byref(self._h), n_row, n_col, batch, precision_code(precision), flag))
+        own = ctypes.c_void_p()
+        _capi.check(lib.hpxfft_plan_get_stream(self._h, ctypes.byref(own)))
+        self._own_stream = own.value
         self.n_row, self.n_col, self.batch = int(n_row), int(n_col), int(batch)
         self.precision = precision_code(precision)
         self.dtype = real_dtype(precision)
@@ -63,7 +66,9 @@ class Plan:
 
     # -- execution
     def set_stream(self, stream_handle: int | None) -> None:
-        _capi.check(self._lib.hpxfft_plan_set_stream(self.handle, ctypes.c_void_p(stream_handle or 0)))
+        """Run on a cudaStream_t handle (0 = legacy default stream); None = the plan's own stream."""
+        h = self._own_stream if stream_handle is None else stream_handle
+        _capi.check(self._lib.hpxfft_plan_set_stream(self.handle, ctypes.c_void_p(h)))
 
     def execute_device(self, ptr: int) -> None:
         """In-place forward transform of a device buffer (asynchronous)."""

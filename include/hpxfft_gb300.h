@@ -37,7 +37,7 @@ extern "C" {
 typedef enum {
     HPXFFT_OK = 0,
     HPXFFT_ERR_INVALID_ARG = 1,      /* std::invalid_argument in the reference (bad plan flag) */
-    HPXFFT_ERR_UNSUPPORTED_SIZE = 2, /* odd ny, a factor other than 2, 3, 5, too long a row */
+    HPXFFT_ERR_UNSUPPORTED_SIZE = 2, /* odd ny, a prime factor above 13, too long a row */
     HPXFFT_ERR_ALLOC = 3,            /* device or pinned allocation failed */
     HPXFFT_ERR_CUDA = 4,             /* a CUDA runtime call failed */
     HPXFFT_ERR_TIMEOUT = 5,          /* a bounded device-side wait gave up */
@@ -67,8 +67,11 @@ HPXFFT_API int hpxfft_plan_create(hpxfft_plan *plan, size_t n_row, size_t n_col,
  * Replaces: ~loop / fftw_adapter::cleanup (core/include/hpxfft/shared/loop.hpp:30). */
 HPXFFT_API int hpxfft_plan_destroy(hpxfft_plan plan);
 
-/* Use a caller-owned cudaStream_t (NULL restores the plan's own stream). */
+/* Run on a caller-owned cudaStream_t, taken verbatim (NULL is the legacy
+ * default stream).  A new plan runs on a non-blocking stream of its own,
+ * whose handle hpxfft_plan_get_stream returns before any set_stream. */
 HPXFFT_API int hpxfft_plan_set_stream(hpxfft_plan plan, void *cuda_stream);
+HPXFFT_API int hpxfft_plan_get_stream(hpxfft_plan plan, void **cuda_stream);
 
 /* Bytes of one array in HBM (n_row * n_col * sizeof(real)) times batch. */
 HPXFFT_API int hpxfft_plan_buffer_bytes(hpxfft_plan plan, size_t *bytes);

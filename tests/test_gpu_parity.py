@@ -45,6 +45,7 @@ def test_kat_4x6_all_precisions(gpu_lib, cuda):
 
 
 SMALL = [(1, 2), (2, 4), (3, 6), (4, 4), (5, 10), (8, 8), (6, 12), (16, 30), (20, 24), (12, 40),
+         (7, 14), (8, 14), (11, 22), (13, 26), (21, 44), (77, 130), (143, 182),
          (64, 128), (96, 160), (128, 256), (256, 256), (384, 640), (640, 384), (1, 1024), (1024, 2)]
 
 
@@ -175,6 +176,7 @@ def test_backward_matches_oracle_adjoint(gpu_lib, cuda, oracle_lib, prec):
 
 
 def test_unsupported_factor_is_rejected(gpu_lib, cuda):
-    with pytest.raises(gpu_lib.HpxFftError) as e:
-        gpu_lib.Plan(7, 16, 1, "f64", "estimate")
-    assert e.value.status == gpu_lib._capi.HPXFFT_ERR_UNSUPPORTED_SIZE
+    for n_row, n_col in ((17, 16), (16, 36), (19 * 2, 8)):  # primes above 13
+        with pytest.raises(gpu_lib.HpxFftError) as e:
+            gpu_lib.Plan(n_row, n_col, 1, "f64", "estimate")
+        assert e.value.status == gpu_lib._capi.HPXFFT_ERR_UNSUPPORTED_SIZE
