@@ -93,12 +93,42 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_LIB
 
 
+CPP_PROGRAMS = {
+    # the drop-in C++ API: the reference's tests and its shared-loop driver
+    "test_dropin": os.path.join(REPO, "tests", "cpp", "test_dropin.cpp"),
+    "hpxfft_gpu_shared_loop": os.path.join(PKG_DIR, "examples", "shared_loop_2d.cpp"),
+}
+
+
+def build_cpp(force: bool = False) -> dict:
+    """C++ programs against the drop-in headers, linked to the library."""
+    cxx = shutil.which("g++") or "c++"
+    inc = [f"-I{os.path.join(REPO, 'include')}", f"-I{os.path.join(PKG_DIR, 'include')}"]
+    hdrs = []
+    for root, _, files in os.walk(os.path.join(PKG_DIR, "include")):
+        hdrs += [os.path.join(root, f) for f in files]
+    out = {}
+    cmds = []
+    for name, src in CPP_PROGRAMS.items():
+        exe = os.path.join(BUILD, name)
+        out[name] = exe
+        if not force and _newer(exe, [src, LIB, *hdrs]):
+            continue
+        cmds.append([cxx, "-std=c++17", "-O2", *inc, "-o", exe, src, f"-L{BUILD}", "-lhpxfft_gb300",
+                     f"-Wl,-rpath,{BUILD}"])
+    with ThreadPoolExecutor(max_workers=max(1, len(cmds))) as ex:
+        for _ in ex.map(_run, cmds):
+            pass
+    return out
+
+
 def build_all(force: bool = False) -> None:
     with ThreadPoolExecutor(max_workers=2) as ex:
         f1 = ex.submit(build_library, force)
         f2 = ex.submit(build_oracle, force)
         f1.result()
         f2.result()
+    build_cpp(force)
 
 
 if __name__ == "__main__":

@@ -29,12 +29,16 @@ struct PassPlan {
 
 // Compute-type traits: T = arithmetic type, S = storage (HBM) real type.
 // kFixedChains: compile-time pass chains are instantiated for this type.
+// kEPTFixed: elements per thread of the compile-time chains (also their
+// largest radix); they run 1024-thread CTAs.  Runtime-plan kernels keep 16
+// elements per thread and kMaxThreads threads.
 struct ArithF32 {
     using T = float;
     using S = float;
     static constexpr bool kScaled = false;
     static constexpr bool kFixedChains = true;
     static constexpr int kMaxThreads = 1024;
+    static constexpr int kEPTFixed = 16;
 };
 struct ArithF64 {
     using T = double;
@@ -42,6 +46,7 @@ struct ArithF64 {
     static constexpr bool kScaled = false;
     static constexpr bool kFixedChains = false;
     static constexpr int kMaxThreads = 512;
+    static constexpr int kEPTFixed = 8;
 };
 struct ArithFF {
     using T = ff;
@@ -49,24 +54,31 @@ struct ArithFF {
     static constexpr bool kScaled = true;  // per-transform power-of-two scale
     static constexpr bool kFixedChains = true;
     static constexpr int kMaxThreads = 512;
+    static constexpr int kEPTFixed = 8;  // 32 data registers: 64-register budget, 32 warps per SM
 };
+constexpr int kFixedThreadsMax = 1024;
 
 // Elements held per thread in every pass (16 complex values).
 constexpr int kElemsPerThread = 16;
 
 // ----------------------------------------------------------------- storage
+// Data moves with streaming cache hints (.cs): each element is read and
+// written once per pass, and keeping it out of L1 leaves L1 to the twiddles.
+__device__ __forceinline__ double2 ld_stream(const double *p) { return __ldcs(reinterpret_cast<const double2 *>(p)); }
+__device__ __forceinline__ float2 ld_stream(const float *p) { return __ldcs(reinterpret_cast<const float2 *>(p)); }
+
 template <class A>
 __device__ __forceinline__ cpx<typename A::T> load_c(const typename A::S *p, int E)
 {
     using S = typename A::S;
     if constexpr (A::kScaled) {
-        const double2 v = *reinterpret_cast<const double2 *>(p);
+        const double2 v = ld_stream(p);
         return cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
     } else if constexpr (sizeof(S) == 8) {
-        const double2 v = *reinterpret_cast<const double2 *>(p);
+        const double2 v = ld_stream(p);
         return cpx<double>{v.x, v.y};
     } else {
-        const float2 v = *reinterpret_cast<const float2 *>(p);
+        const float2 v = ld_stream(p);
         return cpx<float>{v.x, v.y};
     }
 }
@@ -78,11 +90,11 @@ __device__ __forceinline__ void store_c(typename A::S *p, cpx<typename A::T> v, 
         double2 o;
         o.x = ff_to_double(renorm(v.re), E);
         o.y = ff_to_double(renorm(v.im), E);
-        *reinterpret_cast<double2 *>(p) = o;
+        __stcs(reinterpret_cast<double2 *>(p), o);
     } else if constexpr (sizeof(typename A::S) == 8) {
-        *reinterpret_cast<double2 *>(p) = make_double2(v.re, v.im);
+        __stcs(reinterpret_cast<double2 *>(p), make_double2(v.re, v.im));
     } else {
-        *reinterpret_cast<float2 *>(p) = make_float2(v.re, v.im);
+        __stcs(reinterpret_cast<float2 *>(p), make_float2(v.re, v.im));
     }
 }
 
@@ -176,8 +188,9 @@ __device__ void local_fft(cpx<T> *s, int L, int log2W, const PassPlan &pp, const
 // register allocator sees straight-line code.  Twiddles come from per-pass
 // tables laid out [r-1][k] (one coalesced load per r across a warp):
 //   ptab_p[(r-1)*Ls + k] = W_{Ls*R}^{r*k},  r in [1,R), k in [0,Ls).
-template <class T, int R, int L, int W, int NT, int DIR, int Ls>
-__device__ __forceinline__ void fixed_pass(cpx<T> *s, const cpx<T> *__restrict__ tp)
+template <class T, int R, int L, int W, int NT, int DIR, int Ls, bool RAW, bool POST>
+__device__ __forceinline__ void fixed_pass(cpx<T> *s, const cpx<T> *__restrict__ tp, const int *sEc,
+                                           const cpx<T> *__restrict__ post_tw, int post_mult)
 {
     constexpr int LR = L / R;
     constexpr int NTASK = LR * W;
@@ -188,14 +201,34 @@ __device__ __forceinline__ void fixed_pass(cpx<T> *s, const cpx<T> *__restrict__
         const int task = threadIdx.x + t * NT;
         if (NTASK % NT == 0 || task < NTASK) {
             const int w = task % W, jj = task / W;
+            if constexpr (RAW) {
+                // first pass of the float-float path: the slots still hold the
+                // raw doubles; convert with the transform's scale exponent
+                const int E = scale_exp(sEc[w]);
 #pragma unroll
-            for (int r = 0; r < R; ++r) v[t][r] = s[pidx((jj + r * LR) * W + w)];
+                for (int r = 0; r < R; ++r) {
+                    const double2 d = reinterpret_cast<const double2 *>(s)[pidx((jj + r * LR) * W + w)];
+                    v[t][r] = cpx<T>{ff_from_double(d.x, E), ff_from_double(d.y, E)};
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r) v[t][r] = s[pidx((jj + r * LR) * W + w)];
+            }
             if constexpr (Ls > 1) {
                 const int k = jj % Ls;
 #pragma unroll
                 for (int r = 1; r < R; ++r) v[t][r] = cmul(v[t][r], twid<DIR>(tp, (r - 1) * Ls + k));
             }
             DFT<R, DIR, T>::run(v[t]);
+            if constexpr (POST) {
+                // last pass of a cluster-split transform: W_N^(c k2) for output k2
+                if (post_mult) {
+                    const int k = jj % Ls;
+                    const int base = (jj - k) * R + k;
+#pragma unroll
+                    for (int r = 0; r < R; ++r) v[t][r] = cmul(v[t][r], twid<DIR>(post_tw, post_mult * (base + r * Ls)));
+                }
+            }
         }
     }
     __syncthreads();
@@ -213,35 +246,27 @@ __device__ __forceinline__ void fixed_pass(cpx<T> *s, const cpx<T> *__restrict__
     __syncthreads();
 }
 
-__host__ __device__ constexpr int fixed_radix(int L, int Ls) { return (L / Ls) >= 16 ? 16 : L / Ls; }
+__host__ __device__ constexpr int fixed_radix(int L, int Ls, int maxR) { return (L / Ls) >= maxR ? maxR : L / Ls; }
 
-template <class T, int L, int W, int NT, int DIR, int Ls, int Off>
+template <class T, int L, int W, int NT, int DIR, int MAXR, int Ls, int Off, bool RAW, bool POST>
 struct FixedPasses {
-    static __device__ __forceinline__ void run(cpx<T> *s, const cpx<T> *__restrict__ ptab)
+    static __device__ __forceinline__ void run(cpx<T> *s, const cpx<T> *__restrict__ ptab, const int *sEc,
+                                               const cpx<T> *__restrict__ post_tw, int post_mult)
     {
         if constexpr (Ls < L) {
-            constexpr int R = fixed_radix(L, Ls);
-            fixed_pass<T, R, L, W, NT, DIR, Ls>(s, ptab + Off);
-            FixedPasses<T, L, W, NT, DIR, Ls * R, Off + (Ls > 1 ? Ls * (R - 1) : 0)>::run(s, ptab);
+            constexpr int R = fixed_radix(L, Ls, MAXR);
+            constexpr bool last = Ls * R == L;
+            fixed_pass<T, R, L, W, NT, DIR, Ls, RAW && Ls == 1, POST && last>(s, ptab + Off, sEc, post_tw, post_mult);
+            FixedPasses<T, L, W, NT, DIR, MAXR, Ls * R, Off + (Ls > 1 ? Ls * (R - 1) : 0), RAW, POST>::run(
+                s, ptab, sEc, post_tw, post_mult);
         }
     }
 };
 
-// threads of a fixed-length CTA: 16 elements each
-__host__ __device__ constexpr int fixed_threads(int L, int log2W)
+// threads of a fixed-length CTA: EPT elements each, a multiple of 32
+__host__ __device__ constexpr int fixed_threads(int L, int log2W, int EPT)
 {
-    return ((L << log2W) / kElemsPerThread + 31) / 32 * 32 < 32 ? 32 : ((L << log2W) / kElemsPerThread + 31) / 32 * 32;
-}
-
-// Either the compile-time chain (FL > 0) or the runtime radix plan.
-template <class T, int DIR, int FL, int FW>
-__device__ __forceinline__ void run_local_fft(cpx<T> *s, int L, int log2W, const PassPlan &pp,
-                                              const cpx<T> *__restrict__ tw, int Ltab, const cpx<T> *__restrict__ ptab)
-{
-    if constexpr (FL > 0)
-        FixedPasses<T, FL, (1 << FW), fixed_threads(FL, FW), DIR, 1, 0>::run(s, ptab);
-    else
-        local_fft<T, DIR>(s, L, log2W, pp, tw, Ltab);
+    return ((L << log2W) / EPT + 31) / 32 * 32 < 32 ? 32 : ((L << log2W) / EPT + 31) / 32 * 32;
 }
 
 // Largest input exponent per interleaved transform w, reduced over the CTA and
@@ -298,17 +323,48 @@ struct ColArgs {
     const void *ptab;         // per-pass twiddles of the compile-time chain
 };
 
+// The local transform of one CTA: the compile-time chain when FL > 0 (with
+// the float-float conversion fused into its first pass when RAW, and the
+// cluster twiddle W_N^(c k2) fused into its last pass when C > 1), else the
+// runtime radix plan followed by a separate cluster-twiddle sweep.
+// post_mult * k2 indexes the full table for W_N^(c k2).
+template <class A, int DIR, int C, int FL, int FW, bool RAW>
+__device__ __forceinline__ void local_stage(cpx<typename A::T> *s, int L, int log2W, const PassPlan &pp,
+                                            const cpx<typename A::T> *__restrict__ tw, int Ltab,
+                                            const cpx<typename A::T> *__restrict__ ptab, const int *sEc, int post_mult)
+{
+    using T = typename A::T;
+    if constexpr (FL > 0) {
+        constexpr int EPT = A::kEPTFixed;
+        FixedPasses<T, FL, (1 << FW), fixed_threads(FL, FW, EPT), DIR, EPT, 1, 0, RAW, (C > 1)>::run(s, ptab, sEc, tw,
+                                                                                                      post_mult);
+    } else {
+        local_fft<T, DIR>(s, L, log2W, pp, tw, Ltab);
+        if constexpr (C > 1) {
+            if (post_mult) {
+                const int nel = L << log2W;
+                for (int t = threadIdx.x; t < nel; t += blockDim.x)
+                    s[pidx(t)] = cnorm(cmul(s[pidx(t)], twid<DIR>(tw, post_mult * (t >> log2W))));
+            }
+            __syncthreads();
+        }
+    }
+}
+
 // Kernel shape parameters: C = CTAs per cluster, FL = compile-time local
 // length (0: runtime plan), FW = log2 of the interleave when FL > 0.
 #define HPXFFT_SHAPE                                                                      \
     constexpr bool kFixed = FL > 0;                                                       \
+    constexpr int EPT = kFixed ? A::kEPTFixed : kElemsPerThread;                          \
     const int log2W = kFixed ? FW : a.log2W;                                              \
     const int W = 1 << log2W, wmask = W - 1;                                              \
     const int tid = threadIdx.x;                                                          \
-    const int nth = kFixed ? fixed_threads(FL, FW) : (int)blockDim.x;                     \
+    const int nth = kFixed ? fixed_threads(FL, FW, EPT) : (int)blockDim.x;                \
     unsigned crank = 0;                                                                   \
     if constexpr (C > 1) crank = cg::this_cluster().block_rank();                         \
     (void)kFixed;
+
+#define HPXFFT_BOUNDS(A, FL) __launch_bounds__((FL) > 0 ? kFixedThreadsMax : A::kMaxThreads, 1)
 
 // ------------------------------------------------------------ row r2c kernel
 // Packed-real row transform: z[m] = x[2m] + i x[2m+1], Z = DFT_M(z), then
@@ -317,7 +373,7 @@ struct ColArgs {
 // Replaces the FFTW row pass core/src/shared/loop.cpp:61-69 (fft_1d_r2c_inplace,
 // loop.cpp:6-9); output row kx holds X[kx][0..M] in place of the padded input.
 template <class A, int C, int FL, int FW>
-__global__ void __launch_bounds__(A::kMaxThreads, 1) row_r2c_kernel(RowArgs a)
+__global__ void HPXFFT_BOUNDS(A, FL) row_r2c_kernel(RowArgs a)
 {
     using T = typename A::T;
     using S = typename A::S;
@@ -341,18 +397,17 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_r2c_kernel(RowArgs a)
         for (int t = tid; t < nel; t += nth) {
             const int w = t & wmask, m = t >> log2W, row = row0 + w;
             double2 v = make_double2(0.0, 0.0);
-            if (row < a.nrows) {
-                const long long n = crank + (long long)C * m;
-                v = *reinterpret_cast<const double2 *>(in + row * a.in_stride + 2 * n);
-            }
+            if (row < a.nrows) v = ld_stream(in + row * a.in_stride + 2 * (crank + (long long)C * m));
             reinterpret_cast<double2 *>(s)[pidx(t)] = v;
             emax = max(emax, max(dbl_biased_exp(v.x), dbl_biased_exp(v.y)));
         }
         reduce_exponents<C>(emax, log2W, sE, sEc);
-        for (int t = tid; t < nel; t += nth) {
-            const double2 v = reinterpret_cast<double2 *>(s)[pidx(t)];
-            const int E = scale_exp(sEc[t & wmask]);
-            s[pidx(t)] = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
+        if constexpr (!kFixed) {
+            for (int t = tid; t < nel; t += nth) {
+                const double2 v = reinterpret_cast<double2 *>(s)[pidx(t)];
+                const int E = scale_exp(sEc[t & wmask]);
+                s[pidx(t)] = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
+            }
         }
     } else {
         for (int t = tid; t < nel; t += nth) {
@@ -364,7 +419,8 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_r2c_kernel(RowArgs a)
     }
     __syncthreads();
 
-    run_local_fft<T, -1, FL, FW>(s, L, log2W, a.pp, tw, a.Ltab, ptab);
+    // W_M^(c k2) = W_2M^(2 c k2)
+    local_stage<A, -1, C, FL, FW, A::kScaled>(s, L, log2W, a.pp, tw, a.Ltab, ptab, sEc, 2 * (int)crank);
 
     if constexpr (C == 1) {
         const int ntask = (M / 2 + 1) << log2W;
@@ -383,12 +439,9 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_r2c_kernel(RowArgs a)
     } else {
         cg::cluster_group cl = cg::this_cluster();
         const int E = A::kScaled ? scale_exp(sEc[0]) : 0;
-        // W_M^(c k2) = W_2M^(2 c k2)
-        if (crank > 0)
-            for (int t = tid; t < L; t += nth) s[pidx(t)] = cnorm(cmul(s[pidx(t)], tw[2 * (int)crank * t]));
         cl.sync();
         const int Lc = L / C, k20 = crank * Lc;
-        constexpr int TPT = kElemsPerThread / C;
+        constexpr int TPT = (EPT + C - 1) / C;
         cpx<T> v[TPT][C];
 #pragma unroll
         for (int u = 0; u < TPT; ++u) {
@@ -437,7 +490,7 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_r2c_kernel(RowArgs a)
 // adjoint of the r2c.  No reference counterpart (the FFTW backward direction
 // is declared in core/include/hpxfft/util/adapter_fftw.hpp:11 but unused).
 template <class A, int C, int FL, int FW>
-__global__ void __launch_bounds__(A::kMaxThreads, 1) row_c2r_kernel(RowArgs a)
+__global__ void HPXFFT_BOUNDS(A, FL) row_c2r_kernel(RowArgs a)
 {
     using T = typename A::T;
     using S = typename A::S;
@@ -463,8 +516,8 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_c2r_kernel(RowArgs a)
             const int k = crank + C * m;
             double2 v = make_double2(0.0, 0.0), u = make_double2(0.0, 0.0);
             if (row < a.nrows) {
-                v = *reinterpret_cast<const double2 *>(in + row * a.in_stride + 2 * (long long)k);
-                u = *reinterpret_cast<const double2 *>(in + row * a.in_stride + 2 * (long long)(M - k));
+                v = ld_stream(in + row * a.in_stride + 2 * (long long)k);
+                u = ld_stream(in + row * a.in_stride + 2 * (long long)(M - k));
             }
             reinterpret_cast<double2 *>(s)[pidx(t)] = v;
             emax = max(emax, max(max(dbl_biased_exp(v.x), dbl_biased_exp(v.y)),
@@ -499,7 +552,7 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_c2r_kernel(RowArgs a)
     }
     __syncthreads();
 
-    run_local_fft<T, +1, FL, FW>(s, L, log2W, a.pp, tw, a.Ltab, ptab);
+    local_stage<A, +1, C, FL, FW, false>(s, L, log2W, a.pp, tw, a.Ltab, ptab, sEc, 2 * (int)crank);
 
     if constexpr (C == 1) {
         for (int t = tid; t < nel; t += nth) {
@@ -515,9 +568,6 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_c2r_kernel(RowArgs a)
     } else {
         cg::cluster_group cl = cg::this_cluster();
         const int E = A::kScaled ? scale_exp(sEc[0]) : 0;
-        if (crank > 0)
-            for (int t = tid; t < L; t += nth)
-                s[pidx(t)] = cnorm(cmul(s[pidx(t)], twid<+1>(tw, 2 * (int)crank * t)));
         cl.sync();
         const int Lc = L / C, k20 = crank * Lc;
         for (int t = tid; t < Lc; t += nth) {
@@ -543,7 +593,7 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) row_c2r_kernel(RowArgs a)
 // array.  Replaces transpose -> FFTW c2c -> transpose back
 // (core/src/shared/loop.cpp:72-102, fft_1d_c2c_inplace loop.cpp:11-15).
 template <class A, int C, int DIR, int FL, int FW>
-__global__ void __launch_bounds__(A::kMaxThreads, 1) col_kernel(ColArgs a)
+__global__ void HPXFFT_BOUNDS(A, FL) col_kernel(ColArgs a)
 {
     using T = typename A::T;
     using S = typename A::S;
@@ -565,18 +615,17 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) col_kernel(ColArgs a)
         for (int t = tid; t < nel; t += nth) {
             const int w = t & wmask, m = t >> log2W, col = col0 + w;
             double2 v = make_double2(0.0, 0.0);
-            if (col < a.ncols) {
-                const long long n = crank + (long long)C * m;
-                v = *reinterpret_cast<const double2 *>(data + n * a.row_stride + 2 * (long long)col);
-            }
+            if (col < a.ncols) v = ld_stream(data + (crank + (long long)C * m) * a.row_stride + 2 * (long long)col);
             reinterpret_cast<double2 *>(s)[pidx(t)] = v;
             emax = max(emax, max(dbl_biased_exp(v.x), dbl_biased_exp(v.y)));
         }
         reduce_exponents<C>(emax, log2W, sE, sEc);
-        for (int t = tid; t < nel; t += nth) {
-            const double2 v = reinterpret_cast<double2 *>(s)[pidx(t)];
-            const int E = scale_exp(sEc[t & wmask]);
-            s[pidx(t)] = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
+        if constexpr (!kFixed) {
+            for (int t = tid; t < nel; t += nth) {
+                const double2 v = reinterpret_cast<double2 *>(s)[pidx(t)];
+                const int E = scale_exp(sEc[t & wmask]);
+                s[pidx(t)] = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
+            }
         }
     } else {
         for (int t = tid; t < nel; t += nth) {
@@ -589,7 +638,7 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) col_kernel(ColArgs a)
     }
     __syncthreads();
 
-    run_local_fft<T, DIR, FL, FW>(s, L, log2W, a.pp, tw, a.Ltab, ptab);
+    local_stage<A, DIR, C, FL, FW, A::kScaled>(s, L, log2W, a.pp, tw, a.Ltab, ptab, sEc, (int)crank);
 
     if constexpr (C == 1) {
         for (int t = tid; t < nel; t += nth) {
@@ -600,11 +649,6 @@ __global__ void __launch_bounds__(A::kMaxThreads, 1) col_kernel(ColArgs a)
         }
     } else {
         cg::cluster_group cl = cg::this_cluster();
-        if (crank > 0)
-            for (int t = tid; t < nel; t += nth) {
-                const int k2 = t >> log2W;
-                s[pidx(t)] = cnorm(cmul(s[pidx(t)], twid<DIR>(tw, (int)crank * k2)));
-            }
         cl.sync();
         const int Lc = L / C, k20 = crank * Lc;
         const int ntask = Lc << log2W;

@@ -183,12 +183,16 @@ static bool has_fixed(int prec, bool rows, const DimPlan &d)
     }
 }
 
+// elements per thread (= largest radix) of the compile-time chains
+static int fixed_ept(int prec) { return prec == HPXFFT_PREC_F32 ? ArithF32::kEPTFixed : ArithFF::kEPTFixed; }
+
 // (Ls, R) of every pass of the compile-time chain for length L, in order
-static std::vector<std::pair<int, int>> fixed_chain(int L)
+// (the same rule as FixedPasses: the largest radix, then the remainder)
+static std::vector<std::pair<int, int>> fixed_chain(int L, int maxR)
 {
     std::vector<std::pair<int, int>> v;
     for (int Ls = 1; Ls < L;) {
-        const int R = (L / Ls) >= 16 ? 16 : L / Ls;
+        const int R = fixed_radix(L, Ls, maxR);
         v.push_back({Ls, R});
         Ls *= R;
     }
@@ -227,7 +231,7 @@ static int setup_fixed(hpxfft_plan_s &p, DimPlan &d, bool rows, cudaStream_t st)
 {
     d.FL = 0;
     if (!has_fixed(p.prec, rows, d)) return HPXFFT_OK;
-    const auto chain = fixed_chain(d.L);
+    const auto chain = fixed_chain(d.L, fixed_ept(p.prec));
     size_t entries = 0;
     for (auto &c : chain)
         if (c.first > 1) entries += (size_t)c.first * (c.second - 1);
@@ -243,6 +247,7 @@ static int setup_fixed(hpxfft_plan_s &p, DimPlan &d, bool rows, cudaStream_t st)
         off += (size_t)c.first * (c.second - 1);
     }
     d.FL = d.L;
+    d.shape.threads = fixed_threads(d.L, d.log2W, fixed_ept(p.prec));
     return HPXFFT_OK;
 }
 

@@ -94,3 +94,29 @@ def test_bad_plan_flag_throws_invalid_argument(gpu_lib, cuda):
     with pytest.raises(ValueError):
         gpu_lib.shared.loop().initialize(values, "quick")
     assert values.size() == 24  # nothing was moved
+
+
+def test_cpp_dropin_headers(gpu_lib, cuda, build_mod):
+    """The reference's C++ tests compiled against the drop-in headers."""
+    import subprocess
+
+    exe = build_mod.build_cpp()["test_dropin"]
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "all drop-in checks passed" in r.stdout
+
+
+def test_cpp_shared_loop_driver(gpu_lib, cuda, build_mod, tmp_path):
+    """hpxfft_gpu_shared_loop keeps the reference driver's CLI and output files."""
+    import subprocess
+
+    exe = build_mod.build_cpp()["hpxfft_gpu_shared_loop"]
+    r = subprocess.run([exe, "--nx=64", "--ny", "96", "--plan=estimate", "--header=1"], capture_output=True,
+                       text=True, timeout=300, cwd=tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "FFT 2D runtime:" in r.stdout
+    rows = (tmp_path / "runtimes" / "runtimes_hpx_shared_loop.txt").read_text().splitlines()
+    assert rows[0].startswith("n_threads;n_x;n_y;plan;run_flag;total;")
+    assert rows[1].split(";")[1:5] == ["64", "96", "estimate", "par"]
+    plan = (tmp_path / "plans" / "plan_hpx_shared_loop.txt").read_text()
+    assert "GPU r2c 1D plan:" in plan and "GPU c2c 1D plan:" in plan
