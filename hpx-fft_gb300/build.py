@@ -59,17 +59,18 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(REPO, "include", "hpxfft_gb300.h"))
-    srcs = [os.path.join(CSRC, s) for s in SOURCES]
-    if not force and _newer(LIB, srcs + headers + [__file__]):
-        return LIB
     nvcc = _nvcc()
     objs = []
     cmds = []
-    for s in srcs:
-        o = os.path.join(BUILD, os.path.basename(s).replace(".cu", ".o"))
-        objs.append(o)
-        cmds.append([nvcc, *ARCH, *NVCC_FLAGS, "-c", s, "-o", o])
-    with ThreadPoolExecutor(max_workers=len(cmds)) as ex:
+    for name in SOURCES:
+        src = os.path.join(CSRC, name)
+        obj = os.path.join(BUILD, name.replace(".cu", ".o"))
+        objs.append(obj)
+        if force or not _newer(obj, [src, *headers]):
+            cmds.append([nvcc, *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj])
+    if not cmds and os.path.exists(LIB) and _newer(LIB, objs):
+        return LIB
+    with ThreadPoolExecutor(max_workers=max(1, len(cmds))) as ex:
         for _ in ex.map(_run, cmds):
             pass
     tmp = LIB + ".tmp"

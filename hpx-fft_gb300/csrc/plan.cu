@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <vector>
 #include <string>
 
@@ -22,6 +23,7 @@
 namespace hpxfft_gpu {
 
 static thread_local std::string g_last_error;
+constexpr int kMaxDevices = 64;
 
 static int fail(int status, const std::string &msg)
 {
@@ -161,14 +163,23 @@ static bool plan_cols(hpxfft_plan_s &p)
     return false;
 }
 
+// Kernel attributes (dynamic shared memory limit, 16-CTA clusters) belong to
+// the device's context: set them once per device and compute type.
 template <class A>
 static cudaError_t prepare_once()
 {
-    static cudaError_t status = []() {
-        cudaError_t e = RowLaunch<A>::prepare();
-        return e != cudaSuccess ? e : ColLaunch<A>::prepare();
-    }();
-    return status;
+    static std::mutex mu;
+    static bool done[kMaxDevices] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done[dev]) return cudaSuccess;
+    e = RowLaunch<A>::prepare();
+    if (e == cudaSuccess) e = ColLaunch<A>::prepare();
+    if (e == cudaSuccess) done[dev] = true;
+    return e;
 }
 
 static bool has_fixed(int prec, bool rows, const DimPlan &d)
