@@ -692,3 +692,180 @@ int hpxfft_host_free(void *ptr)
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free forward transform (hpxfft_execute_r2c_noalloc).
+//
+// The plan API allocates device memory (twiddle tables) when a plan is
+// created.  Some callers cannot do that: an application whose own pool
+// allocator has reserved all device memory up front (a cudaMalloc then fails
+// or fragments the pool), or a latency-critical pipeline that must not issue
+// cudaMalloc / cudaFree because they can synchronise the whole device.  This
+// entry point serves them: the FP64 transform with the same kernels, its
+// twiddle tables written into one file-scope __device__ array that every GPU
+// loading the library holds until the process exits.
+// ---------------------------------------------------------------------------
+namespace hpxfft_gpu {
+
+constexpr size_t kNoAllocMaxLen = 16384;                  // largest n_row and largest ny
+constexpr size_t kNoAllocScratchBytes = (size_t)1 << 20;  // 1 MiB: 4 tables of <= 16384 pairs
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+static std::mutex g_noalloc_mutex;
+static void *g_noalloc_ptr[kMaxDevices];  // device address of g_noalloc_scratch, per device
+
+// factorize() without a heap allocation: the same radix rule into PassPlan
+static bool noalloc_factorize(int L, PassPlan &pp)
+{
+    int odd[kMaxPasses], nodd = 0, rest = L;
+    for (int q : {3, 5, 7, 11, 13})
+        while (rest % q == 0 && nodd < kMaxPasses) rest /= q, odd[nodd++] = q;
+    if (rest & (rest - 1)) return false;
+    int p2 = 0;
+    while ((1 << p2) < rest) ++p2;
+    pp.n = 0;
+    while (p2 >= 4 && pp.n < kMaxPasses) pp.radix[pp.n++] = 16, p2 -= 4;
+    if (p2 > 0 && pp.n < kMaxPasses) pp.radix[pp.n++] = 1 << p2;
+    for (int i = 0; i < nodd && pp.n < kMaxPasses; ++i) pp.radix[pp.n++] = odd[i];
+    return pp.n < kMaxPasses;
+}
+
+// The same shapes as plan_rows / plan_cols for the float-float type.
+static bool noalloc_shape(hpxfft_plan_s &p)
+{
+    const int maxel = kElemsPerThread * ArithFF::kMaxThreads;
+    for (int C : {1, 2, 4}) {
+        if (p.M % C) continue;
+        const int L = (int)(p.M / C);
+        if ((C > 1 && L % C) || L > maxel) continue;
+        if (!noalloc_factorize(L, p.row.pp)) return false;
+        int log2W = 0;
+        if (C == 1)
+            while (log2W < 4 && (L << (log2W + 1)) <= 4096 && ((size_t)1 << log2W) < p.nx) ++log2W;
+        p.row.C = C;
+        p.row.L = L;
+        p.row.log2W = log2W;
+        const int nel = L << log2W;
+        p.row.shape.threads = threads_for(nel);
+        p.row.shape.smem = (size_t)padded_elems(nel) * 16;
+        p.row.shape.cluster = C;
+        p.row.shape.grid = dim3((unsigned)(((p.nx + ((size_t)1 << log2W) - 1) >> log2W) * C), 1, 1);
+        break;
+    }
+    if (p.row.L == 0) return false;
+    int log2W = 2;
+    while (log2W > 0 && ((size_t)1 << (log2W - 1)) >= p.dcy) --log2W;
+    for (int C : {1, 2, 4, 8, 16}) {
+        if (p.nx % C) continue;
+        const int L = (int)(p.nx / C);
+        if ((C > 1 && L % C) || (L << log2W) > maxel) continue;
+        if (!noalloc_factorize(L, p.col.pp)) return false;
+        p.col.C = C;
+        p.col.L = L;
+        p.col.log2W = log2W;
+        const int nel = L << log2W;
+        p.col.shape.threads = threads_for(nel);
+        p.col.shape.smem = (size_t)padded_elems(nel) * 16;
+        p.col.shape.cluster = C;
+        p.col.shape.grid = dim3((unsigned)(((p.dcy + ((size_t)1 << log2W) - 1) >> log2W) * C), 1, 1);
+        break;
+    }
+    return p.col.L != 0;
+}
+
+// Per-pass tables of a compile-time chain written at `dst` (no allocation).
+static cudaError_t noalloc_fixed_tables(DimPlan &d, bool rows, unsigned char *dst, size_t cap, size_t &used,
+                                        cudaStream_t st)
+{
+    d.FL = 0;
+    used = 0;
+    if (!(rows ? RowLaunch<ArithFF>::has_fixed(d.L, d.log2W, d.C) : ColLaunch<ArithFF>::has_fixed(d.L, d.log2W, d.C)))
+        return cudaSuccess;
+    size_t off = 0;
+    for (int Ls = 1; Ls < d.L;) {
+        const int R = fixed_radix(d.L, Ls, ArithFF::kEPTFixed);
+        if (Ls > 1) {
+            if ((off + (size_t)Ls * (R - 1)) * 16 > cap) return cudaErrorInvalidValue;
+            cudaError_t e = TwiddleLaunch<ArithFF>::pass(dst + off * 16, Ls, R, st);
+            if (e != cudaSuccess) return e;
+            off += (size_t)Ls * (R - 1);
+        }
+        Ls *= R;
+    }
+    d.ptab = dst;
+    d.FL = d.L;
+    d.shape.threads = fixed_threads(d.L, d.log2W, ArithFF::kEPTFixed);
+    used = (off * 16 + 255) & ~(size_t)255;
+    return cudaSuccess;
+}
+
+}  // namespace hpxfft_gpu
+
+extern "C" int hpxfft_execute_r2c_noalloc(const void *d_in, void *d_out, size_t n_row, size_t n_col, void *stream)
+{
+    using namespace hpxfft_gpu;
+    if (!d_in || !d_out) return fail(HPXFFT_ERR_INVALID_ARG, "null device buffer");
+    if (((uintptr_t)d_in | (uintptr_t)d_out) & 15) return fail(HPXFFT_ERR_INVALID_ARG, "buffers must be 16-byte aligned");
+    if (n_row == 0) return fail(HPXFFT_ERR_INVALID_ARG, "empty array");
+    if (n_col < 4 || n_col % 2) return fail(HPXFFT_ERR_UNSUPPORTED_SIZE, "n_col must be 2*(ny/2+1) with ny >= 2 even");
+    if (n_row > kNoAllocMaxLen || n_col - 2 > kNoAllocMaxLen)
+        return fail(HPXFFT_ERR_UNSUPPORTED_SIZE,
+                    "hpxfft_execute_r2c_noalloc handles n_row <= 16384 and ny <= 16384 (its 1 MiB static scratch); "
+                    "use a plan for larger arrays");
+    hpxfft_plan_s p;
+    p.nx = n_row;
+    p.dcy = n_col / 2;
+    p.ny = 2 * p.dcy - 2;
+    p.M = p.ny / 2;
+    p.ncol = n_col;
+    p.batch = 1;
+    p.prec = HPXFFT_PREC_F64;
+    p.real_bytes = 8;
+    p.tw_elem = 16;
+    if (!noalloc_shape(p))
+        return fail(HPXFFT_ERR_UNSUPPORTED_SIZE, "sizes must have no prime factor above 13");
+
+    // one-time set-up per device, with that device current: the device
+    // address of the static scratch array and the kernel attributes
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) return fail(HPXFFT_ERR_CUDA, "device index out of range");
+    unsigned char *base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_ptr[dev]) {
+            void *ptr = nullptr;
+            e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
+            g_noalloc_ptr[dev] = ptr;
+        }
+        base = static_cast<unsigned char *>(g_noalloc_ptr[dev]);
+    }
+    if ((e = prepare_once<ArithFF>()) != cudaSuccess) return cuda_fail(e, "kernel attributes");
+
+    // carve the scratch: full row table (2M pairs), full column table (nx
+    // pairs), then the per-pass tables; every table is rewritten by this call
+    cudaStream_t st = (cudaStream_t)stream;
+    size_t off = 0;
+    p.tw_row = base + off;
+    off += ((2 * p.M * 16) + 255) & ~(size_t)255;
+    p.tw_col = base + off;
+    off += ((p.nx * 16) + 255) & ~(size_t)255;
+    size_t used = 0;
+    if ((e = noalloc_fixed_tables(p.row, true, base + off, kNoAllocScratchBytes - off, used, st)) != cudaSuccess)
+        return cuda_fail(e, "row twiddles");
+    off += used;
+    if ((e = noalloc_fixed_tables(p.col, false, base + off, kNoAllocScratchBytes - off, used, st)) != cudaSuccess)
+        return cuda_fail(e, "column twiddles");
+    off += used;
+    if (off > kNoAllocScratchBytes) return fail(HPXFFT_ERR_UNSUPPORTED_SIZE, "scratch too small");
+    if ((e = TwiddleLaunch<ArithFF>::full(p.tw_row, (int)(2 * p.M), st)) != cudaSuccess ||
+        (e = TwiddleLaunch<ArithFF>::full(p.tw_col, (int)p.nx, st)) != cudaSuccess)
+        return cuda_fail(e, "twiddle generation");
+    if ((e = RowLaunch<ArithFF>::r2c(row_args(p, d_in, d_out, 0), p.row.shape, p.row.FL, st)) != cudaSuccess)
+        return cuda_fail(e, "row kernel");
+    if ((e = ColLaunch<ArithFF>::run(col_args(p, d_out), -1, p.col.shape, p.col.FL, st)) != cudaSuccess)
+        return cuda_fail(e, "column kernel");
+    return HPXFFT_OK;
+}

@@ -48,6 +48,7 @@ SIGNATURES = {
     "hpxfft_plan_flag_valid": (_ci, [_cs]),
     "hpxfft_status_string": (_cs, [_ci]),
     "hpxfft_last_error": (_cs, []),
+    "hpxfft_execute_r2c_noalloc": (_ci, [_vp, _vp, _sz, _sz, _vp]),
     "hpxfft_host_alloc": (_ci, [ctypes.POINTER(_vp), _sz]),
     "hpxfft_host_free": (_ci, [_vp]),
 }

@@ -132,6 +132,23 @@ HPXFFT_API int hpxfft_plan_flag_valid(const char *plan_flag);
 HPXFFT_API const char *hpxfft_status_string(int status);
 HPXFFT_API const char *hpxfft_last_error(void);
 
+/* Forward FP64 transform that allocates nothing, for callers that cannot
+ * allocate device memory: an application whose pool allocator already holds
+ * all device memory (cudaMalloc would fail or fragment it), or a pipeline
+ * that must not call cudaMalloc / cudaFree because they can synchronise the
+ * whole device.  d_in and d_out are caller-owned device buffers in the padded
+ * layout (they may be equal); the transform is queued on `stream` (NULL is
+ * the legacy default stream) and nothing is synchronised.
+ * Limits: n_row <= 16384 and ny = n_col - 2 <= 16384, FP64 only; larger
+ * sizes return HPXFFT_ERR_UNSUPPORTED_SIZE.  The twiddle tables live in one
+ * 1 MiB static __device__ array that each GPU loading the library keeps
+ * until the process exits; every call rewrites it, so calls that overlap on
+ * the GPU (other streams, other threads) race and must be serialised by the
+ * caller.  The first call on a device does a one-time set-up (it looks up
+ * the array's device address and sets kernel attributes); make that first
+ * call before any stream capture.  No counterpart in the reference. */
+HPXFFT_API int hpxfft_execute_r2c_noalloc(const void *d_in, void *d_out, size_t n_row, size_t n_col, void *stream);
+
 /* Pinned host memory for fast host<->device copies (cudaHostAlloc). */
 HPXFFT_API int hpxfft_host_alloc(void **ptr, size_t bytes);
 HPXFFT_API int hpxfft_host_free(void *ptr);
