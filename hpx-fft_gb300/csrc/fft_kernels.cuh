@@ -54,9 +54,13 @@ struct ArithFF {
     static constexpr bool kScaled = true;  // per-transform power-of-two scale
     static constexpr bool kFixedChains = true;
     static constexpr int kMaxThreads = 512;
-    static constexpr int kEPTFixed = 8;  // 32 data registers: 64-register budget, 32 warps per SM
+    static constexpr int kEPTFixed = 8;  // 32 data registers within the 64-register budget
 };
-constexpr int kFixedThreadsMax = 1024;
+// Compile-time chains run at most 512 threads with a 64-register budget, so
+// two CTAs (and their <= 64 KB of data) share an SM: one streams its strip
+// in or out while the other computes.
+constexpr int kFixedThreadsMax = 512;
+constexpr int kFixedMinBlocks = 2;
 
 // Elements held per thread in every pass (16 complex values).
 constexpr int kElemsPerThread = 16;
@@ -269,6 +273,27 @@ __host__ __device__ constexpr int fixed_threads(int L, int log2W, int EPT)
     return ((L << log2W) / EPT + 31) / 32 * 32 < 32 ? 32 : ((L << log2W) / EPT + 31) / 32 * 32;
 }
 
+// Loads of a thread are issued back to back before any is consumed, so a CTA
+// keeps BATCH loads per thread in flight instead of waiting one DRAM latency
+// per element.  ld(t) loads element t, use(t, v) consumes it.
+template <int BATCH, class V, class LD, class USE>
+__device__ __forceinline__ void batched_loop(int nel, int nth, LD ld, USE use)
+{
+    for (int base = threadIdx.x; base < nel; base += BATCH * nth) {
+        V v[BATCH];
+#pragma unroll
+        for (int i = 0; i < BATCH; ++i) {
+            const int t = base + i * nth;
+            if (t < nel) v[i] = ld(t);
+        }
+#pragma unroll
+        for (int i = 0; i < BATCH; ++i) {
+            const int t = base + i * nth;
+            if (t < nel) use(t, v[i]);
+        }
+    }
+}
+
 // Largest input exponent per interleaved transform w, reduced over the CTA and
 // (C > 1) over the cluster.  Every thread's elements share w = tid & (W-1).
 template <int C>
@@ -364,7 +389,8 @@ __device__ __forceinline__ void local_stage(cpx<typename A::T> *s, int L, int lo
     if constexpr (C > 1) crank = cg::this_cluster().block_rank();                         \
     (void)kFixed;
 
-#define HPXFFT_BOUNDS(A, FL) __launch_bounds__((FL) > 0 ? kFixedThreadsMax : A::kMaxThreads, 1)
+#define HPXFFT_BOUNDS(A, FL) \
+    __launch_bounds__((FL) > 0 ? kFixedThreadsMax : A::kMaxThreads, (FL) > 0 ? kFixedMinBlocks : 1)
 
 // ------------------------------------------------------------ row r2c kernel
 // Packed-real row transform: z[m] = x[2m] + i x[2m+1], Z = DFT_M(z), then
@@ -379,7 +405,7 @@ __global__ void HPXFFT_BOUNDS(A, FL) row_r2c_kernel(RowArgs a)
     using S = typename A::S;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cpx<T> *s = reinterpret_cast<cpx<T> *>(smem_raw);
-    __shared__ int sE[16], sEc[16];
+    __shared__ int sE[64], sEc[64];
     HPXFFT_SHAPE
     const int M = a.M;
     const int L = kFixed ? FL : M / C;
@@ -390,17 +416,21 @@ __global__ void HPXFFT_BOUNDS(A, FL) row_r2c_kernel(RowArgs a)
     const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
     const cpx<T> *ptab = reinterpret_cast<const cpx<T> *>(a.ptab);
 
+    auto ld_row = [&](int t) {
+        using V2 = typename std::conditional<sizeof(S) == 8, double2, float2>::type;
+        const int w = t & wmask, m = t >> log2W, row = row0 + w;
+        V2 v{};
+        if (row < a.nrows) v = ld_stream(in + row * a.in_stride + 2 * (crank + (long long)C * m));
+        return v;
+    };
     if constexpr (A::kScaled) {
-        if (tid < 16) sE[tid] = 0;
+        if (tid < 64) sE[tid] = 0;
         __syncthreads();
         int emax = 0;
-        for (int t = tid; t < nel; t += nth) {
-            const int w = t & wmask, m = t >> log2W, row = row0 + w;
-            double2 v = make_double2(0.0, 0.0);
-            if (row < a.nrows) v = ld_stream(in + row * a.in_stride + 2 * (crank + (long long)C * m));
+        batched_loop<EPT, double2>(nel, nth, ld_row, [&](int t, double2 v) {
             reinterpret_cast<double2 *>(s)[pidx(t)] = v;
             emax = max(emax, max(dbl_biased_exp(v.x), dbl_biased_exp(v.y)));
-        }
+        });
         reduce_exponents<C>(emax, log2W, sE, sEc);
         if constexpr (!kFixed) {
             for (int t = tid; t < nel; t += nth) {
@@ -410,12 +440,8 @@ __global__ void HPXFFT_BOUNDS(A, FL) row_r2c_kernel(RowArgs a)
             }
         }
     } else {
-        for (int t = tid; t < nel; t += nth) {
-            const int w = t & wmask, m = t >> log2W, row = row0 + w;
-            cpx<T> v = czero<T>();
-            if (row < a.nrows) v = load_c<A>(in + row * a.in_stride + 2 * (crank + (long long)C * m), 0);
-            s[pidx(t)] = v;
-        }
+        using V2 = typename std::conditional<sizeof(S) == 8, double2, float2>::type;
+        batched_loop<EPT, V2>(nel, nth, ld_row, [&](int t, V2 v) { s[pidx(t)] = cpx<T>{(T)v.x, (T)v.y}; });
     }
     __syncthreads();
 
@@ -496,7 +522,7 @@ __global__ void HPXFFT_BOUNDS(A, FL) row_c2r_kernel(RowArgs a)
     using S = typename A::S;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cpx<T> *s = reinterpret_cast<cpx<T> *>(smem_raw);
-    __shared__ int sE[16], sEc[16];
+    __shared__ int sE[64], sEc[64];
     HPXFFT_SHAPE
     const int M = a.M;
     const int L = kFixed ? FL : M / C;
@@ -509,20 +535,25 @@ __global__ void HPXFFT_BOUNDS(A, FL) row_c2r_kernel(RowArgs a)
 
     int emax = 0;
     if constexpr (A::kScaled) {
-        if (tid < 16) sE[tid] = 0;
+        if (tid < 64) sE[tid] = 0;
         __syncthreads();
-        for (int t = tid; t < nel; t += nth) {
-            const int w = t & wmask, m = t >> log2W, row = row0 + w;
-            const int k = crank + C * m;
-            double2 v = make_double2(0.0, 0.0), u = make_double2(0.0, 0.0);
-            if (row < a.nrows) {
-                v = ld_stream(in + row * a.in_stride + 2 * (long long)k);
-                u = ld_stream(in + row * a.in_stride + 2 * (long long)(M - k));
-            }
-            reinterpret_cast<double2 *>(s)[pidx(t)] = v;
-            emax = max(emax, max(max(dbl_biased_exp(v.x), dbl_biased_exp(v.y)),
-                                 max(dbl_biased_exp(u.x), dbl_biased_exp(u.y))));
-        }
+        batched_loop<EPT / 2, double4>(
+            nel, nth,
+            [&](int t) {
+                const int w = t & wmask, m = t >> log2W, row = row0 + w;
+                const int k = crank + C * m;
+                double2 v = make_double2(0.0, 0.0), u = make_double2(0.0, 0.0);
+                if (row < a.nrows) {
+                    v = ld_stream(in + row * a.in_stride + 2 * (long long)k);
+                    u = ld_stream(in + row * a.in_stride + 2 * (long long)(M - k));
+                }
+                return make_double4(v.x, v.y, u.x, u.y);
+            },
+            [&](int t, double4 q) {
+                reinterpret_cast<double2 *>(s)[pidx(t)] = make_double2(q.x, q.y);
+                emax = max(emax, max(max(dbl_biased_exp(q.x), dbl_biased_exp(q.y)),
+                                     max(dbl_biased_exp(q.z), dbl_biased_exp(q.w))));
+            });
         reduce_exponents<C>(emax, log2W, sE, sEc);
     }
     for (int t = tid; t < nel; t += nth) {
@@ -599,7 +630,7 @@ __global__ void HPXFFT_BOUNDS(A, FL) col_kernel(ColArgs a)
     using S = typename A::S;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cpx<T> *s = reinterpret_cast<cpx<T> *>(smem_raw);
-    __shared__ int sE[16], sEc[16];
+    __shared__ int sE[64], sEc[64];
     HPXFFT_SHAPE
     const int L = kFixed ? FL : a.nx / C;
     const int nel = L << log2W;
@@ -608,17 +639,21 @@ __global__ void HPXFFT_BOUNDS(A, FL) col_kernel(ColArgs a)
     const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
     const cpx<T> *ptab = reinterpret_cast<const cpx<T> *>(a.ptab);
 
+    using V2 = typename std::conditional<sizeof(S) == 8, double2, float2>::type;
+    auto ld_col = [&](int t) {
+        const int w = t & wmask, m = t >> log2W, col = col0 + w;
+        V2 v{};
+        if (col < a.ncols) v = ld_stream(data + (crank + (long long)C * m) * a.row_stride + 2 * (long long)col);
+        return v;
+    };
     if constexpr (A::kScaled) {
-        if (tid < 16) sE[tid] = 0;
+        if (tid < 64) sE[tid] = 0;
         __syncthreads();
         int emax = 0;
-        for (int t = tid; t < nel; t += nth) {
-            const int w = t & wmask, m = t >> log2W, col = col0 + w;
-            double2 v = make_double2(0.0, 0.0);
-            if (col < a.ncols) v = ld_stream(data + (crank + (long long)C * m) * a.row_stride + 2 * (long long)col);
+        batched_loop<EPT, double2>(nel, nth, ld_col, [&](int t, double2 v) {
             reinterpret_cast<double2 *>(s)[pidx(t)] = v;
             emax = max(emax, max(dbl_biased_exp(v.x), dbl_biased_exp(v.y)));
-        }
+        });
         reduce_exponents<C>(emax, log2W, sE, sEc);
         if constexpr (!kFixed) {
             for (int t = tid; t < nel; t += nth) {
@@ -628,13 +663,7 @@ __global__ void HPXFFT_BOUNDS(A, FL) col_kernel(ColArgs a)
             }
         }
     } else {
-        for (int t = tid; t < nel; t += nth) {
-            const int w = t & wmask, m = t >> log2W, col = col0 + w;
-            cpx<T> v = czero<T>();
-            if (col < a.ncols)
-                v = load_c<A>(data + (crank + (long long)C * m) * a.row_stride + 2 * (long long)col, 0);
-            s[pidx(t)] = v;
-        }
+        batched_loop<EPT, V2>(nel, nth, ld_col, [&](int t, V2 v) { s[pidx(t)] = cpx<T>{(T)v.x, (T)v.y}; });
     }
     __syncthreads();
 
@@ -666,6 +695,98 @@ __global__ void HPXFFT_BOUNDS(A, FL) col_kernel(ColArgs a)
             }
         }
         cl.sync();
+    }
+}
+
+// ------------------------------------------------------ column step kernel
+// One step of a two-kernel four-step column FFT, nx = N1 * N2:
+//   step A (group g = n1):  in rows g + N1*m  -> DFT_N2 over m, times W_nx^(g k)
+//                           -> out rows g + N1*k
+//   step B (group g = k2):  in rows N1*g + m  -> DFT_N1 over m
+//                           -> out rows g + N2*k        (natural order)
+// Each CTA owns a strip of W adjacent columns (W * 16 bytes per row segment)
+// and never waits on another CTA.  A reads the data and writes a scratch
+// array of the same layout, B reads the scratch and writes the data, so the
+// column pass costs two HBM round trips instead of one but streams wide
+// segments with full occupancy.
+struct ColStepArgs {
+    const void *in;
+    void *out;
+    long long row_stride;     // reals per row (both arrays)
+    long long in_bstride, out_bstride;
+    int ncols;
+    int strips;               // column strips per group
+    int in_step, out_step;    // row steps of m and k
+    int in_gmul, out_gmul;    // row offset of group g: g * gmul
+    int post;                 // multiply by W_nx^(g k) (step A)
+    int L;                    // DFT length of this step
+    int log2W;
+    PassPlan pp;
+    const void *tw;           // W_nx table (post twiddle) and runtime-plan twiddles
+    int Ltab;                 // nx
+    const void *ptab;
+};
+
+template <class A, int DIR, int FL, int FW>
+__global__ void HPXFFT_BOUNDS(A, FL) colstep_kernel(ColStepArgs a)
+{
+    using T = typename A::T;
+    using S = typename A::S;
+    constexpr int C = 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cpx<T> *s = reinterpret_cast<cpx<T> *>(smem_raw);
+    __shared__ int sE[64], sEc[64];
+    HPXFFT_SHAPE
+    const int L = kFixed ? FL : a.L;
+    const int nel = L << log2W;
+    const int g = blockIdx.x / a.strips, col0 = (blockIdx.x % a.strips) * W;
+    const S *in = reinterpret_cast<const S *>(a.in) + (long long)blockIdx.y * a.in_bstride;
+    S *out = reinterpret_cast<S *>(a.out) + (long long)blockIdx.y * a.out_bstride;
+    const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
+    const cpx<T> *ptab = reinterpret_cast<const cpx<T> *>(a.ptab);
+    const long long in_row0 = (long long)g * a.in_gmul, out_row0 = (long long)g * a.out_gmul;
+
+    using V2 = typename std::conditional<sizeof(S) == 8, double2, float2>::type;
+    auto ld = [&](int t) {
+        const int w = t & wmask, m = t >> log2W, col = col0 + w;
+        V2 v{};
+        if (col < a.ncols) v = ld_stream(in + (in_row0 + (long long)a.in_step * m) * a.row_stride + 2 * (long long)col);
+        return v;
+    };
+    if constexpr (A::kScaled) {
+        if (tid < 64) sE[tid] = 0;
+        __syncthreads();
+        int emax = 0;
+        batched_loop<EPT, double2>(nel, nth, ld, [&](int t, double2 v) {
+            reinterpret_cast<double2 *>(s)[pidx(t)] = v;
+            emax = max(emax, max(dbl_biased_exp(v.x), dbl_biased_exp(v.y)));
+        });
+        reduce_exponents<1>(emax, log2W, sE, sEc);
+        if constexpr (!kFixed) {
+            for (int t = tid; t < nel; t += nth) {
+                const double2 v = reinterpret_cast<double2 *>(s)[pidx(t)];
+                const int E = scale_exp(sEc[t & wmask]);
+                s[pidx(t)] = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
+            }
+        }
+    } else {
+        batched_loop<EPT, V2>(nel, nth, ld, [&](int t, V2 v) { s[pidx(t)] = cpx<T>{(T)v.x, (T)v.y}; });
+    }
+    __syncthreads();
+
+    if constexpr (kFixed)
+        FixedPasses<T, FL, (1 << FW), fixed_threads(FL, FW, EPT), DIR, EPT, 1, 0, A::kScaled, false>::run(
+            s, ptab, sEc, tw, 0);
+    else
+        local_fft<T, DIR>(s, L, log2W, a.pp, tw, a.Ltab);
+
+    for (int t = tid; t < nel; t += nth) {
+        const int w = t & wmask, k = t >> log2W, col = col0 + w;
+        if (col >= a.ncols) continue;
+        const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
+        cpx<T> v = s[pidx(t)];
+        if (a.post && g) v = cmul(v, twid<DIR>(tw, g * k));
+        store_c<A>(out + (out_row0 + (long long)a.out_step * k) * a.row_stride + 2 * (long long)col, v, E);
     }
 }
 

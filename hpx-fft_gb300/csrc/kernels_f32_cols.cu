@@ -4,4 +4,5 @@
 
 namespace hpxfft_gpu {
 template struct ColLaunch<ArithF32>;
+template struct ColStepLaunch<ArithF32>;
 }

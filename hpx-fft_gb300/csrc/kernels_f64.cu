@@ -7,4 +7,5 @@
 namespace hpxfft_gpu {
 template struct RowLaunch<ArithF64>;
 template struct ColLaunch<ArithF64>;
+template struct ColStepLaunch<ArithF64>;
 }

@@ -4,4 +4,5 @@
 
 namespace hpxfft_gpu {
 template struct ColLaunch<ArithFF>;
+template struct ColStepLaunch<ArithFF>;
 }

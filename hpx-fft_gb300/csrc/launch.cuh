@@ -15,12 +15,17 @@ struct LaunchShape {
     int cluster;
 };
 
-// Compile-time configurations (local length L, log2 interleave, cluster size).
-// Rows: L >= 4096 one row per CTA, shorter rows packed up to 4096 elements.
-#define HPXFFT_ROW_FIXED_COMMON(X) X(8192, 0, 1) X(8192, 0, 2) X(4096, 0, 1) X(2048, 1, 1) X(1024, 2, 1) X(512, 3, 1) X(256, 4, 1)
-#define HPXFFT_ROW_FIXED_F32(X) X(16384, 0, 1)
-// Columns: power-of-two nx >= 2048 always splits into local length 2048.
-#define HPXFFT_COL_FIXED(X, LW) X(2048, LW, 1) X(2048, LW, 2) X(2048, LW, 4) X(2048, LW, 8) X(2048, LW, 16)
+// Compile-time configurations (local length L, log2 interleave, cluster size)
+// for power-of-two sizes: at most 4096 float-float or 8192 FP32 elements per
+// CTA (64 KB of data), the shapes the planner picks.
+// Rows: one row per CTA up to that size (shorter rows packed), longer rows
+// split over a cluster.
+#define HPXFFT_ROW_FIXED_FF(X) X(4096, 0, 1) X(4096, 0, 2) X(4096, 0, 4) X(2048, 1, 1) X(1024, 2, 1) X(512, 3, 1) X(256, 4, 1)
+#define HPXFFT_ROW_FIXED_F32(X) X(8192, 0, 1) X(8192, 0, 2) X(4096, 1, 1) X(2048, 2, 1) X(1024, 3, 1) X(512, 4, 1)
+// Columns: strips of 4 (float-float) or 8 (FP32) columns, 64-byte row
+// segments; nx >= 2048 splits into local length 1024 over 2..16 CTAs.
+#define HPXFFT_COL_FIXED_FF(X) X(256, 2, 1) X(512, 2, 1) X(1024, 2, 1) X(1024, 2, 2) X(1024, 2, 4) X(1024, 2, 8) X(1024, 2, 16) X(2048, 1, 16)
+#define HPXFFT_COL_FIXED_F32(X) X(512, 3, 1) X(1024, 3, 1) X(1024, 3, 2) X(1024, 3, 4) X(1024, 3, 8) X(1024, 3, 16) X(2048, 2, 16)
 
 template <class A>
 struct RowLaunch {
@@ -37,6 +42,18 @@ struct ColLaunch {
     static cudaError_t prepare();
     static bool has_fixed(int L, int log2W, int C);
     static cudaError_t run(const ColArgs &a, int dir, const LaunchShape &s, int FL, cudaStream_t st);
+};
+
+// Two-kernel column steps: (DFT length, log2 strip width), strips of up to 64
+// columns (512-byte float-float / FP32 segments of 32 / 64 columns).
+#define HPXFFT_COLSTEP_FIXED_FF(X) X(32, 6) X(64, 6) X(128, 5) X(256, 4)
+#define HPXFFT_COLSTEP_FIXED_F32(X) X(32, 6) X(64, 6) X(128, 6) X(256, 5)
+
+template <class A>
+struct ColStepLaunch {
+    static cudaError_t prepare();
+    static bool has_fixed(int L, int log2W);
+    static cudaError_t run(const ColStepArgs &a, int dir, const LaunchShape &s, int FL, cudaStream_t st);
 };
 
 template <class A>
@@ -93,8 +110,11 @@ cudaError_t RowLaunch<A>::prepare()
 #define HPXFFT_X(L, W, C)                                                  \
     HPXFFT_TRY(set_attrs(row_r2c_kernel<A, C, L, W>, false));              \
     HPXFFT_TRY(set_attrs(row_c2r_kernel<A, C, L, W>, false));
-        HPXFFT_ROW_FIXED_COMMON(HPXFFT_X)
-        if constexpr (sizeof(typename A::S) == 4) { HPXFFT_ROW_FIXED_F32(HPXFFT_X) }
+        if constexpr (sizeof(typename A::S) == 4) {
+            HPXFFT_ROW_FIXED_F32(HPXFFT_X)
+        } else {
+            HPXFFT_ROW_FIXED_FF(HPXFFT_X)
+        }
 #undef HPXFFT_X
     }
     return cudaSuccess;
@@ -106,8 +126,11 @@ bool RowLaunch<A>::has_fixed(int L, int log2W, int C)
     if constexpr (!A::kFixedChains) return false;
 #define HPXFFT_X(L_, W_, C_) \
     if (L == L_ && log2W == W_ && C == C_) return true;
-    HPXFFT_ROW_FIXED_COMMON(HPXFFT_X)
-    if constexpr (sizeof(typename A::S) == 4) { HPXFFT_ROW_FIXED_F32(HPXFFT_X) }
+    if constexpr (sizeof(typename A::S) == 4) {
+        HPXFFT_ROW_FIXED_F32(HPXFFT_X)
+    } else {
+        HPXFFT_ROW_FIXED_FF(HPXFFT_X)
+    }
 #undef HPXFFT_X
     return false;
 }
@@ -119,8 +142,11 @@ cudaError_t RowLaunch<A>::r2c(const RowArgs &a, const LaunchShape &s, int FL, cu
         if (FL) {
 #define HPXFFT_X(L_, W_, C_) \
     if (FL == L_ && a.log2W == W_ && s.cluster == C_) return launch_cluster(row_r2c_kernel<A, C_, L_, W_>, a, s, st);
-            HPXFFT_ROW_FIXED_COMMON(HPXFFT_X)
-            if constexpr (sizeof(typename A::S) == 4) { HPXFFT_ROW_FIXED_F32(HPXFFT_X) }
+            if constexpr (sizeof(typename A::S) == 4) {
+                HPXFFT_ROW_FIXED_F32(HPXFFT_X)
+            } else {
+                HPXFFT_ROW_FIXED_FF(HPXFFT_X)
+            }
 #undef HPXFFT_X
             return cudaErrorInvalidValue;
         }
@@ -140,8 +166,11 @@ cudaError_t RowLaunch<A>::c2r(const RowArgs &a, const LaunchShape &s, int FL, cu
         if (FL) {
 #define HPXFFT_X(L_, W_, C_) \
     if (FL == L_ && a.log2W == W_ && s.cluster == C_) return launch_cluster(row_c2r_kernel<A, C_, L_, W_>, a, s, st);
-            HPXFFT_ROW_FIXED_COMMON(HPXFFT_X)
-            if constexpr (sizeof(typename A::S) == 4) { HPXFFT_ROW_FIXED_F32(HPXFFT_X) }
+            if constexpr (sizeof(typename A::S) == 4) {
+                HPXFFT_ROW_FIXED_F32(HPXFFT_X)
+            } else {
+                HPXFFT_ROW_FIXED_FF(HPXFFT_X)
+            }
 #undef HPXFFT_X
             return cudaErrorInvalidValue;
         }
@@ -168,7 +197,11 @@ cudaError_t ColLaunch<A>::prepare()
 #define HPXFFT_X(L, W, C)                                                 \
     HPXFFT_TRY(set_attrs(col_kernel<A, C, -1, L, W>, C > 8));             \
     HPXFFT_TRY(set_attrs(col_kernel<A, C, +1, L, W>, C > 8));
-        HPXFFT_COL_FIXED(HPXFFT_X, kLog2W)
+        if constexpr (sizeof(typename A::S) == 4) {
+        HPXFFT_COL_FIXED_F32(HPXFFT_X)
+    } else {
+        HPXFFT_COL_FIXED_FF(HPXFFT_X)
+    }
 #undef HPXFFT_X
     }
     return cudaSuccess;
@@ -180,7 +213,11 @@ bool ColLaunch<A>::has_fixed(int L, int log2W, int C)
     if constexpr (!A::kFixedChains) return false;
 #define HPXFFT_X(L_, W_, C_) \
     if (L == L_ && log2W == W_ && C == C_) return true;
-    HPXFFT_COL_FIXED(HPXFFT_X, kLog2W)
+    if constexpr (sizeof(typename A::S) == 4) {
+        HPXFFT_COL_FIXED_F32(HPXFFT_X)
+    } else {
+        HPXFFT_COL_FIXED_FF(HPXFFT_X)
+    }
 #undef HPXFFT_X
     return false;
 }
@@ -194,7 +231,11 @@ cudaError_t ColLaunch<A>::run(const ColArgs &a, int dir, const LaunchShape &s, i
     if (FL == L_ && a.log2W == W_ && s.cluster == C_)                                     \
         return dir < 0 ? launch_cluster(col_kernel<A, C_, -1, L_, W_>, a, s, st)          \
                        : launch_cluster(col_kernel<A, C_, +1, L_, W_>, a, s, st);
-            HPXFFT_COL_FIXED(HPXFFT_X, kLog2W)
+            if constexpr (sizeof(typename A::S) == 4) {
+        HPXFFT_COL_FIXED_F32(HPXFFT_X)
+    } else {
+        HPXFFT_COL_FIXED_FF(HPXFFT_X)
+    }
 #undef HPXFFT_X
             return cudaErrorInvalidValue;
         }
@@ -208,6 +249,64 @@ cudaError_t ColLaunch<A>::run(const ColArgs &a, int dir, const LaunchShape &s, i
     default: return cudaErrorInvalidValue;
     }
 #undef HPXFFT_G
+}
+#endif
+
+#ifdef HPXFFT_DEFINE_COLS
+template <class A>
+cudaError_t ColStepLaunch<A>::prepare()
+{
+    HPXFFT_TRY(set_attrs(colstep_kernel<A, -1, 0, 0>, false));
+    HPXFFT_TRY(set_attrs(colstep_kernel<A, +1, 0, 0>, false));
+    if constexpr (A::kFixedChains) {
+#define HPXFFT_X(L, W)                                                 \
+    HPXFFT_TRY(set_attrs(colstep_kernel<A, -1, L, W>, false));         \
+    HPXFFT_TRY(set_attrs(colstep_kernel<A, +1, L, W>, false));
+        if constexpr (sizeof(typename A::S) == 4) {
+            HPXFFT_COLSTEP_FIXED_F32(HPXFFT_X)
+        } else {
+            HPXFFT_COLSTEP_FIXED_FF(HPXFFT_X)
+        }
+#undef HPXFFT_X
+    }
+    return cudaSuccess;
+}
+
+template <class A>
+bool ColStepLaunch<A>::has_fixed(int L, int log2W)
+{
+    if constexpr (!A::kFixedChains) return false;
+#define HPXFFT_X(L_, W_) \
+    if (L == L_ && log2W == W_) return true;
+    if constexpr (sizeof(typename A::S) == 4) {
+        HPXFFT_COLSTEP_FIXED_F32(HPXFFT_X)
+    } else {
+        HPXFFT_COLSTEP_FIXED_FF(HPXFFT_X)
+    }
+#undef HPXFFT_X
+    return false;
+}
+
+template <class A>
+cudaError_t ColStepLaunch<A>::run(const ColStepArgs &a, int dir, const LaunchShape &s, int FL, cudaStream_t st)
+{
+    if constexpr (A::kFixedChains) {
+        if (FL) {
+#define HPXFFT_X(L_, W_)                                                              \
+    if (FL == L_ && a.log2W == W_)                                                    \
+        return dir < 0 ? launch_cluster(colstep_kernel<A, -1, L_, W_>, a, s, st)      \
+                       : launch_cluster(colstep_kernel<A, +1, L_, W_>, a, s, st);
+            if constexpr (sizeof(typename A::S) == 4) {
+                HPXFFT_COLSTEP_FIXED_F32(HPXFFT_X)
+            } else {
+                HPXFFT_COLSTEP_FIXED_FF(HPXFFT_X)
+            }
+#undef HPXFFT_X
+            return cudaErrorInvalidValue;
+        }
+    }
+    return dir < 0 ? launch_cluster(colstep_kernel<A, -1, 0, 0>, a, s, st)
+                   : launch_cluster(colstep_kernel<A, +1, 0, 0>, a, s, st);
 }
 #endif
 

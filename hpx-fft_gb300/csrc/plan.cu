@@ -11,6 +11,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -54,6 +55,11 @@ struct hpxfft_plan_s {
     size_t real_bytes = 8;  // bytes of one storage real
     size_t tw_elem = 16;    // bytes of one complex twiddle
     hpxfft_gpu::DimPlan row, col;
+    // two-kernel column pass (nx = N1 * N2): step A then step B through scratch
+    bool col_two_step = false;
+    int N1 = 0, N2 = 0;
+    hpxfft_gpu::DimPlan colA, colB;
+    void *scratch = nullptr;
     void *tw_row = nullptr, *tw_col = nullptr;
     void *dbuf = nullptr;
     size_t dbuf_bytes = 0;
@@ -95,7 +101,9 @@ static bool factorize(int L, int max_radix, PassPlan &pp)
     return true;
 }
 
-static int max_threads_for(int prec) { return prec == HPXFFT_PREC_F32 ? 1024 : 512; }
+// Elements of one CTA's transform(s): 4096 float-float (or FP64) pairs or
+// 8192 FP32 pairs, 64 KB of data, so two CTAs share an SM.
+static int max_elems_for(int prec) { return prec == HPXFFT_PREC_F32 ? 8192 : 4096; }
 
 static int threads_for(int nel)
 {
@@ -104,9 +112,11 @@ static int threads_for(int nel)
     return t < 32 ? 32 : t;
 }
 
+// Rows: the smallest cluster whose CTAs hold a row each; short rows are
+// packed (up to 16 per CTA) to fill the CTA.
 static bool plan_rows(hpxfft_plan_s &p)
 {
-    const int maxel = kElemsPerThread * max_threads_for(p.prec);
+    const int maxel = max_elems_for(p.prec);
     const size_t cbytes = 2 * p.real_bytes;
     for (int C : {1, 2, 4}) {
         if (p.M % C) continue;
@@ -117,7 +127,7 @@ static bool plan_rows(hpxfft_plan_s &p)
         if (!factorize(L, 16, pp)) return false;
         int log2W = 0;
         if (C == 1)
-            while (log2W < 4 && (L << (log2W + 1)) <= 4096 && ((size_t)1 << log2W) < p.nx) ++log2W;
+            while (log2W < 4 && (L << (log2W + 1)) <= maxel && ((size_t)1 << log2W) < p.nx) ++log2W;
         DimPlan &d = p.row;
         d.C = C;
         d.L = L;
@@ -134,33 +144,74 @@ static bool plan_rows(hpxfft_plan_s &p)
     return false;
 }
 
+// Columns: strips as wide as possible (64-byte row segments: 4 float-float
+// or 8 FP32 columns), then the smallest cluster that holds the strip.
 static bool plan_cols(hpxfft_plan_s &p)
 {
-    const int maxel = kElemsPerThread * max_threads_for(p.prec);
+    const int maxel = max_elems_for(p.prec);
     const size_t cbytes = 2 * p.real_bytes;
-    int log2W = p.prec == HPXFFT_PREC_F32 ? 3 : 2;  // 64-byte row segments
-    while (log2W > 0 && ((size_t)1 << (log2W - 1)) >= p.dcy) --log2W;
-    for (int C : {1, 2, 4, 8, 16}) {
-        if (p.nx % C) continue;
-        const int L = (int)(p.nx / C);
-        if (C > 1 && L % C) continue;
-        if ((L << log2W) > maxel) continue;
+    int pref = p.prec == HPXFFT_PREC_F32 ? 3 : 2;
+    while (pref > 0 && ((size_t)1 << (pref - 1)) >= p.dcy) --pref;
+    for (int log2W = pref; log2W >= 0; --log2W) {
+        for (int C : {1, 2, 4, 8, 16}) {
+            if (p.nx % C) continue;
+            const int L = (int)(p.nx / C);
+            if (C > 1 && L % C) continue;
+            if ((L << log2W) > maxel) continue;
+            PassPlan pp;
+            if (!factorize(L, 16, pp)) return false;
+            DimPlan &d = p.col;
+            d.C = C;
+            d.L = L;
+            d.log2W = log2W;
+            d.pp = pp;
+            const int nel = L << log2W;
+            d.shape.threads = threads_for(nel);
+            d.shape.smem = (size_t)padded_elems(nel) * cbytes;
+            d.shape.cluster = C;
+            const size_t strips = (p.dcy + ((size_t)1 << log2W) - 1) >> log2W;
+            d.shape.grid = dim3((unsigned)(strips * C), (unsigned)p.batch, 1);
+            return true;
+        }
+    }
+    return false;
+}
+
+// Shapes of the two-kernel column pass for power-of-two nx >= 1024:
+// N2 = 2^floor(log2(nx)/2) (step A length), N1 = nx / N2 (step B length),
+// strips of up to 64 columns.
+static bool plan_colsteps(hpxfft_plan_s &p)
+{
+    if (p.nx < 1024 || (p.nx & (p.nx - 1))) return false;
+    int lg = 0;
+    while (((size_t)1 << lg) < p.nx) ++lg;
+    p.N2 = 1 << (lg / 2);
+    p.N1 = (int)(p.nx / p.N2);
+    const int maxel = max_elems_for(p.prec);
+    const size_t cbytes = 2 * p.real_bytes;
+    int wcap = 6;  // at most 64 columns per strip
+    while (wcap > 0 && ((size_t)1 << (wcap - 1)) >= p.dcy) --wcap;
+    for (int step = 0; step < 2; ++step) {
+        DimPlan &d = step == 0 ? p.colA : p.colB;
+        const int L = step == 0 ? p.N2 : p.N1;
+        int log2W = wcap;
+        while (log2W > 0 && (L << log2W) > maxel) --log2W;
+        if ((L << log2W) > maxel) return false;
         PassPlan pp;
         if (!factorize(L, 16, pp)) return false;
-        DimPlan &d = p.col;
-        d.C = C;
+        d.C = 1;
         d.L = L;
         d.log2W = log2W;
         d.pp = pp;
         const int nel = L << log2W;
         d.shape.threads = threads_for(nel);
         d.shape.smem = (size_t)padded_elems(nel) * cbytes;
-        d.shape.cluster = C;
+        d.shape.cluster = 1;
         const size_t strips = (p.dcy + ((size_t)1 << log2W) - 1) >> log2W;
-        d.shape.grid = dim3((unsigned)(strips * C), (unsigned)p.batch, 1);
-        return true;
+        const size_t groups = step == 0 ? (size_t)p.N1 : (size_t)p.N2;
+        d.shape.grid = dim3((unsigned)(groups * strips), (unsigned)p.batch, 1);
     }
-    return false;
+    return true;
 }
 
 // Kernel attributes (dynamic shared memory limit, 16-CTA clusters) belong to
@@ -178,8 +229,18 @@ static cudaError_t prepare_once()
     if (done[dev]) return cudaSuccess;
     e = RowLaunch<A>::prepare();
     if (e == cudaSuccess) e = ColLaunch<A>::prepare();
+    if (e == cudaSuccess) e = ColStepLaunch<A>::prepare();
     if (e == cudaSuccess) done[dev] = true;
     return e;
+}
+
+static bool has_fixed_step(int prec, const DimPlan &d)
+{
+    switch (prec) {
+    case HPXFFT_PREC_F64: return ColStepLaunch<ArithFF>::has_fixed(d.L, d.log2W);
+    case HPXFFT_PREC_F32: return ColStepLaunch<ArithF32>::has_fixed(d.L, d.log2W);
+    default: return false;
+    }
 }
 
 static bool has_fixed(int prec, bool rows, const DimPlan &d)
@@ -238,10 +299,10 @@ static cudaError_t gen_pass_twiddles(int prec, void *tab, int Ls, int R, cudaStr
 }
 
 // Allocate and fill the per-pass tables when the dimension uses a fixed chain.
-static int setup_fixed(hpxfft_plan_s &p, DimPlan &d, bool rows, cudaStream_t st)
+static int setup_fixed(hpxfft_plan_s &p, DimPlan &d, bool rows, cudaStream_t st, int step = 0)
 {
     d.FL = 0;
-    if (!has_fixed(p.prec, rows, d)) return HPXFFT_OK;
+    if (!(step ? has_fixed_step(p.prec, d) : has_fixed(p.prec, rows, d))) return HPXFFT_OK;
     const auto chain = fixed_chain(d.L, fixed_ept(p.prec));
     size_t entries = 0;
     for (auto &c : chain)
@@ -312,6 +373,46 @@ static cudaEvent_t *next_slot(hpxfft_plan_s &p)
     return p.kev[p.next % hpxfft_plan_s::kSlots];
 }
 
+static ColStepArgs colstep_args(const hpxfft_plan_s &p, int step, const void *in, void *out)
+{
+    const DimPlan &d = step == 0 ? p.colA : p.colB;
+    ColStepArgs a{};
+    a.in = in;
+    a.out = out;
+    a.row_stride = (long long)p.ncol;
+    a.in_bstride = a.out_bstride = (long long)(p.nx * p.ncol);
+    a.ncols = (int)p.dcy;
+    a.strips = (int)((p.dcy + ((size_t)1 << d.log2W) - 1) >> d.log2W);
+    if (step == 0) {  // rows g + N1 m -> rows g + N1 k, times W_nx^(g k)
+        a.in_step = a.out_step = p.N1;
+        a.in_gmul = a.out_gmul = 1;
+        a.post = 1;
+    } else {  // rows N1 g + m -> rows g + N2 k
+        a.in_step = 1;
+        a.in_gmul = p.N1;
+        a.out_step = p.N2;
+        a.out_gmul = 1;
+        a.post = 0;
+    }
+    a.L = d.L;
+    a.log2W = d.log2W;
+    a.pp = d.pp;
+    a.tw = p.tw_col;
+    a.Ltab = (int)p.nx;
+    a.ptab = d.ptab;
+    return a;
+}
+
+// The column pass, in place on `data`: one cluster kernel or steps A and B.
+template <class A>
+static cudaError_t run_columns(hpxfft_plan_s &p, void *data, int dir)
+{
+    if (!p.col_two_step) return ColLaunch<A>::run(col_args(p, data), dir, p.col.shape, p.col.FL, p.stream);
+    cudaError_t e = ColStepLaunch<A>::run(colstep_args(p, 0, data, p.scratch), dir, p.colA.shape, p.colA.FL, p.stream);
+    if (e != cudaSuccess) return e;
+    return ColStepLaunch<A>::run(colstep_args(p, 1, p.scratch, data), dir, p.colB.shape, p.colB.FL, p.stream);
+}
+
 template <class A>
 static cudaError_t run_forward(hpxfft_plan_s &p, const void *in, void *out)
 {
@@ -320,7 +421,7 @@ static cudaError_t run_forward(hpxfft_plan_s &p, const void *in, void *out)
     if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
     if ((e = RowLaunch<A>::r2c(row_args(p, in, out, 0), p.row.shape, p.row.FL, p.stream)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
-    if ((e = ColLaunch<A>::run(col_args(p, out), -1, p.col.shape, p.col.FL, p.stream)) != cudaSuccess) return e;
+    if ((e = run_columns<A>(p, out, -1)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[2], p.stream)) != cudaSuccess) return e;
     ++p.next;
     return cudaSuccess;
@@ -332,7 +433,7 @@ static cudaError_t run_inverse(hpxfft_plan_s &p, void *data, int adjoint)
     cudaError_t e;
     cudaEvent_t *ev = next_slot(p);
     if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
-    if ((e = ColLaunch<A>::run(col_args(p, data), +1, p.col.shape, p.col.FL, p.stream)) != cudaSuccess) return e;
+    if ((e = run_columns<A>(p, data, +1)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
     if ((e = RowLaunch<A>::c2r(row_args(p, data, data, adjoint), p.row.shape, p.row.FL, p.stream)) != cudaSuccess)
         return e;
@@ -502,6 +603,25 @@ int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
     }
     int rc = setup_fixed(*p, p->row, true, p->stream);
     if (rc == HPXFFT_OK) rc = setup_fixed(*p, p->col, false, p->stream);
+    // column strategy: the two-kernel pass streams 512-byte row segments and
+    // wins once the cluster kernel needs 8 or more CTAs per strip
+    // HPXFFT_COLUMNS=cluster|steps overrides the choice (tuning and tests)
+    const char *force = std::getenv("HPXFFT_COLUMNS");
+    bool want_steps = p->col.C >= 8;
+    if (force && !strcmp(force, "cluster")) want_steps = false;
+    if (force && !strcmp(force, "steps")) want_steps = true;
+    if (rc == HPXFFT_OK && precision != HPXFFT_PREC_F64_NATIVE && want_steps && plan_colsteps(*p)) {
+        rc = setup_fixed(*p, p->colA, false, p->stream, 1);
+        if (rc == HPXFFT_OK) rc = setup_fixed(*p, p->colB, false, p->stream, 2);
+        if (rc == HPXFFT_OK) {
+            if (cudaMalloc(&p->scratch, p->nx * p->ncol * p->real_bytes * p->batch) != cudaSuccess) {
+                cudaGetLastError();
+                rc = fail(HPXFFT_ERR_ALLOC, "column scratch buffer");
+            } else {
+                p->col_two_step = true;
+            }
+        }
+    }
     if (rc != HPXFFT_OK) {
         std::string msg = g_last_error;
         hpxfft_plan_destroy(p);
@@ -533,6 +653,9 @@ int hpxfft_plan_destroy(hpxfft_plan p)
     cudaFree(p->tw_col);
     cudaFree(p->row.ptab);
     cudaFree(p->col.ptab);
+    cudaFree(p->colA.ptab);
+    cudaFree(p->colB.ptab);
+    cudaFree(p->scratch);
     cudaFree(p->dbuf);
     for (auto &slot : p->kev)
         for (auto &ev : slot)
@@ -669,7 +792,13 @@ int hpxfft_write_plan(hpxfft_plan p, const char *path)
     FILE *f = fopen(path, "a");
     if (!f) return fail(HPXFFT_ERR_IO, std::string("Failed to open file: ") + path);
     fprintf(f, "GPU r2c 1D plan:\n%s\n", describe(*p, p->row, "r2c", p->ny).c_str());
-    fprintf(f, "GPU c2c 1D plan:\n%s\n\n", describe(*p, p->col, "c2c", p->nx).c_str());
+    if (p->col_two_step) {
+        fprintf(f, "GPU c2c 1D plan (four-step, %d x %d):\n%s\n%s\n\n", p->N1, p->N2,
+                describe(*p, p->colA, "c2c-stepA", (size_t)p->N2).c_str(),
+                describe(*p, p->colB, "c2c-stepB", (size_t)p->N1).c_str());
+    } else {
+        fprintf(f, "GPU c2c 1D plan:\n%s\n\n", describe(*p, p->col, "c2c", p->nx).c_str());
+    }
     fclose(f);
     return HPXFFT_OK;
 }
@@ -733,7 +862,7 @@ static bool noalloc_factorize(int L, PassPlan &pp)
 // The same shapes as plan_rows / plan_cols for the float-float type.
 static bool noalloc_shape(hpxfft_plan_s &p)
 {
-    const int maxel = kElemsPerThread * ArithFF::kMaxThreads;
+    const int maxel = max_elems_for(HPXFFT_PREC_F64);
     for (int C : {1, 2, 4}) {
         if (p.M % C) continue;
         const int L = (int)(p.M / C);
@@ -741,7 +870,7 @@ static bool noalloc_shape(hpxfft_plan_s &p)
         if (!noalloc_factorize(L, p.row.pp)) return false;
         int log2W = 0;
         if (C == 1)
-            while (log2W < 4 && (L << (log2W + 1)) <= 4096 && ((size_t)1 << log2W) < p.nx) ++log2W;
+            while (log2W < 4 && (L << (log2W + 1)) <= maxel && ((size_t)1 << log2W) < p.nx) ++log2W;
         p.row.C = C;
         p.row.L = L;
         p.row.log2W = log2W;
@@ -753,22 +882,24 @@ static bool noalloc_shape(hpxfft_plan_s &p)
         break;
     }
     if (p.row.L == 0) return false;
-    int log2W = 2;
-    while (log2W > 0 && ((size_t)1 << (log2W - 1)) >= p.dcy) --log2W;
-    for (int C : {1, 2, 4, 8, 16}) {
-        if (p.nx % C) continue;
-        const int L = (int)(p.nx / C);
-        if ((C > 1 && L % C) || (L << log2W) > maxel) continue;
-        if (!noalloc_factorize(L, p.col.pp)) return false;
-        p.col.C = C;
-        p.col.L = L;
-        p.col.log2W = log2W;
-        const int nel = L << log2W;
-        p.col.shape.threads = threads_for(nel);
-        p.col.shape.smem = (size_t)padded_elems(nel) * 16;
-        p.col.shape.cluster = C;
-        p.col.shape.grid = dim3((unsigned)(((p.dcy + ((size_t)1 << log2W) - 1) >> log2W) * C), 1, 1);
-        break;
+    int pref = 2;
+    while (pref > 0 && ((size_t)1 << (pref - 1)) >= p.dcy) --pref;
+    for (int log2W = pref; log2W >= 0 && p.col.L == 0; --log2W) {
+        for (int C : {1, 2, 4, 8, 16}) {
+            if (p.nx % C) continue;
+            const int L = (int)(p.nx / C);
+            if ((C > 1 && L % C) || (L << log2W) > maxel) continue;
+            if (!noalloc_factorize(L, p.col.pp)) return false;
+            p.col.C = C;
+            p.col.L = L;
+            p.col.log2W = log2W;
+            const int nel = L << log2W;
+            p.col.shape.threads = threads_for(nel);
+            p.col.shape.smem = (size_t)padded_elems(nel) * 16;
+            p.col.shape.cluster = C;
+            p.col.shape.grid = dim3((unsigned)(((p.dcy + ((size_t)1 << log2W) - 1) >> log2W) * C), 1, 1);
+            break;
+        }
     }
     return p.col.L != 0;
 }

@@ -87,6 +87,24 @@ def test_cluster_split_transforms(gpu_lib, cuda, oracle_lib, prec):
         assert rel_l2(got, ref) <= TOL[prec], (prec, nx, ny)
 
 
+@pytest.mark.parametrize("strategy", ["cluster", "steps"])
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_column_strategies(gpu_lib, cuda, oracle_lib, monkeypatch, strategy, prec):
+    """Both column passes: one cluster-split kernel, or two four-step kernels through scratch."""
+    monkeypatch.setenv("HPXFFT_COLUMNS", strategy)
+    rng = np.random.default_rng(303)
+    for nx, ny in ((1024, 40), (4096, 64), (8192, 36), (16384, 18), (32768, 10)):
+        x = rng.uniform(-1, 1, (nx, ny))
+        xin = x.astype(np.float32) if prec == "f32" else x
+        got = forward(gpu_lib, cuda, xin, prec)
+        assert rel_l2(got, oracle_fwd(oracle_lib, xin.astype(np.float64))) <= TOL[prec], (strategy, nx, ny)
+        # the inverse runs the same column pass backwards
+        spec = np.ascontiguousarray(got).view(np.float32 if prec == "f32" else np.float64)
+        with gpu_lib.Plan(nx, 2 * (ny // 2 + 1), 1, prec, "estimate") as plan:
+            back = run_device(cuda, plan, spec, "c2r")
+        assert rel_l2(back[:, :ny] / (nx * ny), xin) <= (1e-6 if prec == "f32" else 1e-13)
+
+
 def test_4096_squared_fp64_config_vs_oracle(gpu_lib, cuda, oracle_lib):
     """4096^2 FP64, values uniform[0,1) from a seed: the small drop-in config."""
     x = np.random.default_rng(1).uniform(0, 1, (4096, 4096))
