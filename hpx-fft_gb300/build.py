@@ -32,6 +32,7 @@ SOURCES = [
     "kernels_f64.cu",
     "twiddles.cu",
     "plan.cu",
+    "batch.cu",
 ]
 
 

@@ -66,10 +66,11 @@ constexpr int kFixedMinBlocks = 2;
 constexpr int kElemsPerThread = 16;
 
 // ----------------------------------------------------------------- storage
-// Data moves with streaming cache hints (.cs): each element is read and
-// written once per pass, and keeping it out of L1 leaves L1 to the twiddles.
-__device__ __forceinline__ double2 ld_stream(const double *p) { return __ldcs(reinterpret_cast<const double2 *>(p)); }
-__device__ __forceinline__ float2 ld_stream(const float *p) { return __ldcs(reinterpret_cast<const float2 *>(p)); }
+// Data bypasses L1 (loads .cg, stores .cs): each element is read and written
+// once per pass, L1 stays with the twiddles, and a kernel that reads data
+// another SM wrote in the same launch (the batched work queue) sees it at L2.
+__device__ __forceinline__ double2 ld_stream(const double *p) { return __ldcg(reinterpret_cast<const double2 *>(p)); }
+__device__ __forceinline__ float2 ld_stream(const float *p) { return __ldcg(reinterpret_cast<const float2 *>(p)); }
 
 template <class A>
 __device__ __forceinline__ cpx<typename A::T> load_c(const typename A::S *p, int E)
@@ -398,8 +399,9 @@ __device__ __forceinline__ void local_stage(cpx<typename A::T> *s, int L, int lo
 //   E = (Z[k] + conj Z[M-k]) / 2,  O = (Z[k] - conj Z[M-k]) / 2.
 // Replaces the FFTW row pass core/src/shared/loop.cpp:61-69 (fft_1d_r2c_inplace,
 // loop.cpp:6-9); output row kx holds X[kx][0..M] in place of the padded input.
+// Body of the row r2c for row group `group` of batch item `bidx`.
 template <class A, int C, int FL, int FW>
-__global__ void HPXFFT_BOUNDS(A, FL) row_r2c_kernel(RowArgs a)
+__device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bidx)
 {
     using T = typename A::T;
     using S = typename A::S;
@@ -410,9 +412,9 @@ __global__ void HPXFFT_BOUNDS(A, FL) row_r2c_kernel(RowArgs a)
     const int M = a.M;
     const int L = kFixed ? FL : M / C;
     const int nel = L << log2W;
-    const int row0 = (blockIdx.x / C) * W;
-    const S *in = reinterpret_cast<const S *>(a.in) + (long long)blockIdx.y * a.in_bstride;
-    S *out = reinterpret_cast<S *>(a.out) + (long long)blockIdx.y * a.out_bstride;
+    const int row0 = group * W;
+    const S *in = reinterpret_cast<const S *>(a.in) + (long long)bidx * a.in_bstride;
+    S *out = reinterpret_cast<S *>(a.out) + (long long)bidx * a.out_bstride;
     const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
     const cpx<T> *ptab = reinterpret_cast<const cpx<T> *>(a.ptab);
 
@@ -506,6 +508,12 @@ __global__ void HPXFFT_BOUNDS(A, FL) row_r2c_kernel(RowArgs a)
         }
         cl.sync();
     }
+}
+
+template <class A, int C, int FL, int FW>
+__global__ void HPXFFT_BOUNDS(A, FL) row_r2c_kernel(RowArgs a)
+{
+    row_r2c_body<A, C, FL, FW>(a, blockIdx.x / C, blockIdx.y);
 }
 
 // ------------------------------------------------------------ row c2r kernel
@@ -624,7 +632,7 @@ __global__ void HPXFFT_BOUNDS(A, FL) row_c2r_kernel(RowArgs a)
 // array.  Replaces transpose -> FFTW c2c -> transpose back
 // (core/src/shared/loop.cpp:72-102, fft_1d_c2c_inplace loop.cpp:11-15).
 template <class A, int C, int DIR, int FL, int FW>
-__global__ void HPXFFT_BOUNDS(A, FL) col_kernel(ColArgs a)
+__device__ __forceinline__ void col_body(const ColArgs &a, int strip, int bidx)
 {
     using T = typename A::T;
     using S = typename A::S;
@@ -634,8 +642,8 @@ __global__ void HPXFFT_BOUNDS(A, FL) col_kernel(ColArgs a)
     HPXFFT_SHAPE
     const int L = kFixed ? FL : a.nx / C;
     const int nel = L << log2W;
-    const int col0 = (blockIdx.x / C) * W;
-    S *data = reinterpret_cast<S *>(a.data) + (long long)blockIdx.y * a.bstride;
+    const int col0 = strip * W;
+    S *data = reinterpret_cast<S *>(a.data) + (long long)bidx * a.bstride;
     const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
     const cpx<T> *ptab = reinterpret_cast<const cpx<T> *>(a.ptab);
 
@@ -696,6 +704,12 @@ __global__ void HPXFFT_BOUNDS(A, FL) col_kernel(ColArgs a)
         }
         cl.sync();
     }
+}
+
+template <class A, int C, int DIR, int FL, int FW>
+__global__ void HPXFFT_BOUNDS(A, FL) col_kernel(ColArgs a)
+{
+    col_body<A, C, DIR, FL, FW>(a, blockIdx.x / C, blockIdx.y);
 }
 
 // ------------------------------------------------------ column step kernel

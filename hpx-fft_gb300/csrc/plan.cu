@@ -31,6 +31,8 @@ static int fail(int status, const std::string &msg)
     g_last_error = msg;
     return status;
 }
+int set_error(int status, const std::string &msg) { return fail(status, msg); }
+
 static int cuda_fail(cudaError_t e, const char *what)
 {
     return fail(HPXFFT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));

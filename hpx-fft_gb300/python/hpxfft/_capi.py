@@ -49,6 +49,17 @@ SIGNATURES = {
     "hpxfft_status_string": (_cs, [_ci]),
     "hpxfft_last_error": (_cs, []),
     "hpxfft_execute_r2c_noalloc": (_ci, [_vp, _vp, _sz, _sz, _vp]),
+    "hpxfft_batch_create": (_ci, [ctypes.POINTER(_vp), _sz, ctypes.POINTER(_sz), ctypes.POINTER(_sz), _ci, _cs]),
+    "hpxfft_batch_destroy": (_ci, [_vp]),
+    "hpxfft_batch_arena_bytes": (_ci, [_vp, ctypes.POINTER(_sz)]),
+    "hpxfft_batch_offsets": (_ci, [_vp, ctypes.POINTER(_sz)]),
+    "hpxfft_batch_set_stream": (_ci, [_vp, _vp]),
+    "hpxfft_batch_execute": (_ci, [_vp, _vp]),
+    "hpxfft_batch_synchronize": (_ci, [_vp]),
+    "hpxfft_batch_get_measurement": (_ci, [_vp, _cs, ctypes.POINTER(ctypes.c_double)]),
+    "hpxfft_wisdom_export": (_ci, [_cs]),
+    "hpxfft_wisdom_import": (_ci, [_cs]),
+    "hpxfft_wisdom_forget": (_ci, []),
     "hpxfft_host_alloc": (_ci, [ctypes.POINTER(_vp), _sz]),
     "hpxfft_host_free": (_ci, [_vp]),
 }

@@ -132,6 +132,37 @@ HPXFFT_API int hpxfft_plan_flag_valid(const char *plan_flag);
 HPXFFT_API const char *hpxfft_status_string(int status);
 HPXFFT_API const char *hpxfft_last_error(void);
 
+/* ---- batches of uneven sizes -------------------------------------------
+ * Many independent forward 2D r2c transforms of different shapes in one
+ * persistent work-queue launch, captured in a CUDA graph and replayed.
+ * Instance i is an n_rows[i] x n_cols[i] padded array placed at byte offset
+ * offsets[i] of one device arena (hpxfft_batch_offsets); every row and every
+ * column must fit one CTA (at most 8192 FP32 or 4096 FP64 complex values).
+ * plan_flag "estimate" uses the default queue order; "measure", "patient"
+ * and "exhaustive" time candidate orders on a scratch arena once and cache
+ * the winner for this mix of shapes (see hpxfft_wisdom_*).
+ * No reference counterpart (the reference transforms one array at a time). */
+typedef struct hpxfft_batch_s *hpxfft_batch;
+HPXFFT_API int hpxfft_batch_create(hpxfft_batch *batch, size_t count, const size_t *n_rows, const size_t *n_cols,
+                                   int precision, const char *plan_flag);
+HPXFFT_API int hpxfft_batch_destroy(hpxfft_batch batch);
+HPXFFT_API int hpxfft_batch_arena_bytes(hpxfft_batch batch, size_t *bytes);
+HPXFFT_API int hpxfft_batch_offsets(hpxfft_batch batch, size_t *offsets);
+HPXFFT_API int hpxfft_batch_set_stream(hpxfft_batch batch, void *cuda_stream);
+/* In place on the arena, asynchronous (graph launch on the batch's stream). */
+HPXFFT_API int hpxfft_batch_execute(hpxfft_batch batch, void *d_arena);
+/* Wait for the last execute; HPXFFT_ERR_TIMEOUT if a bounded device wait gave up. */
+HPXFFT_API int hpxfft_batch_synchronize(hpxfft_batch batch);
+/* "total" (s, last execute), "plan" (s), "items", "lag", "ctas_per_sm",
+ * "algorithmic_bytes", "cached_plan". */
+HPXFFT_API int hpxfft_batch_get_measurement(hpxfft_batch batch, const char *name, double *value);
+
+/* Tuned batch configurations, process-wide: write them to / read them from a
+ * text file (the analogue of FFTW wisdom), or drop them. */
+HPXFFT_API int hpxfft_wisdom_export(const char *path);
+HPXFFT_API int hpxfft_wisdom_import(const char *path);
+HPXFFT_API int hpxfft_wisdom_forget(void);
+
 /* Forward FP64 transform that allocates nothing, for callers that cannot
  * allocate device memory: an application whose pool allocator already holds
  * all device memory (cudaMalloc would fail or fragment it), or a pipeline
