@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--precision", default="f64", choices=["f64", "f32", "f64-native"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the FP32 / batch / backward sections")
     args = ap.parse_args()
     args.nx = args.nx or args.n
     args.ny = args.ny or args.n
@@ -307,9 +308,17 @@ def run_ours(args):
     d2h = plan.measurement("d2h")
 
     peak, peak_kind = measured_peak_hbm()
-    dominant = "row" if stats["first"] >= stats["second"] else "column"
-    dom_t = max(stats["first"], stats["second"])
-    per_kernel_bytes = B / 2.0  # each pass reads S and writes S
+    # per launch: every kernel of the step reads S and writes S (B / 2)
+    steps = int(plan.measurement("column_steps"))
+    kernels = {"row_r2c_kernel": stats["first"]}
+    if steps == 2:
+        kernels["colstep_kernel (A)"] = plan.measurement("mean_col_step_a")
+        kernels["colstep_kernel (B)"] = plan.measurement("mean_col_step_b")
+    else:
+        kernels["col_kernel"] = stats["second"]
+    dominant = max(kernels, key=kernels.get)
+    dom_t = kernels[dominant]
+    per_kernel_bytes = B / 2.0
     achieved = per_kernel_bytes / dom_t / 1e9 if dom_t > 0 else 0.0
 
     line = None
@@ -318,6 +327,7 @@ def run_ours(args):
 
         rel = None
         cpu = None
+        oracle_ref = None
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
             cpu = cpu_baseline(nx, ny, x64, threads)
@@ -325,6 +335,7 @@ def run_ours(args):
             oracle.fft_2d_r2c(ref, nthreads=threads)
             refc = ref.view(np.complex128)
             rel = float(np.linalg.norm((spec_out.astype(np.complex128) - refc).ravel()) / np.linalg.norm(refc.ravel()))
+            oracle_ref = refc
         line = {
             "metric": METRIC,
             "value": value,
@@ -349,12 +360,11 @@ def run_ours(args):
                 "parallelism": "replicas" if world > 1 else "single GPU",
                 "rel_l2_vs_oracle": rel,
             },
-            "gpu_launches": 2 * args.steps,
-            "kernels_ms": {"row_r2c": 1e3 * stats["first"], "col_c2c": 1e3 * stats["second"],
-                           "count": stats["count"]},
+            "gpu_launches": (1 + steps) * args.steps,
+            "kernels_ms": dict({k: 1e3 * v for k, v in kernels.items()}, count=stats["count"]),
             "roofline": {
                 "bound": "hbm",
-                "kernel": "row_r2c_kernel" if dominant == "row" else "col_kernel",
+                "kernel": dominant,
                 "achieved": achieved,
                 "peak": peak,
                 "peak_kind": peak_kind,
@@ -376,12 +386,95 @@ def run_ours(args):
         }
         if cpu is not None:
             line["cpu_baseline"] = {k: v for k, v in cpu.items() if k != "seconds"}
+        if not args.no_extras and world == 1:
+            line["extras"] = extras(torch, hpxfft, args, x64, oracle_ref if cpu is not None else None, peak)
         print(json.dumps(line), flush=True)
     plan.close()
     if world > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
     return 0
+
+
+def _time_steps(torch, stream, fn, steps, warmup):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def extras(torch, hpxfft, args, x64, oracle_ref, peak):
+    """The other workloads of this path, measured in the same run:
+    FP32 at the same size (precision), 1024 uneven FP32 transforms in one
+    persistent graph-replayed launch (batching), and the adjoint on 64 FP32
+    2048^2 arrays (differentiation)."""
+    out = {}
+    stream = torch.cuda.current_stream()
+    nx, ny = args.nx, args.ny
+    nc = 2 * (ny // 2 + 1)
+    steps, warm = max(3, args.steps), max(3, args.warmup)
+
+    # precision: FP32 in and out, error against the FP64 oracle
+    x32 = torch.from_numpy(x64.astype(np.float32)).cuda()
+    y32 = torch.empty_like(x32)
+    with hpxfft.Plan(nx, nc, 1, "f32", "estimate") as p32:
+        p32.set_stream(stream.cuda_stream)
+        ms = _time_steps(torch, stream, lambda: p32.execute_oop(x32.data_ptr(), y32.data_ptr()), steps, warm)
+        B = algorithmic_bytes(nx, ny, 4)
+        sec = {"workload": f"2d_r2c_f32_{nx}x{ny}", "ms": ms, "value": B / (ms * 1e-3) / 1e9, "unit": "GB/s",
+               "frac_of_measured_hbm": B / (ms * 1e-3) / 1e9 / peak}
+        if oracle_ref is not None:
+            got = y32.cpu().numpy().view(np.complex64).astype(np.complex128)
+            d = got - oracle_ref
+            sec["rel_l2_vs_fp64_oracle"] = float(np.linalg.norm(d.ravel()) / np.linalg.norm(oracle_ref.ravel()))
+            sec["max_abs_err_vs_fp64_oracle"] = float(np.abs(d).max())
+        out["precision_f32"] = sec
+    del x32, y32
+
+    # batching: 1024 uneven FP32 instances
+    sizes = [256, 384, 512, 640, 768, 1024, 1536, 2048, 2560, 3072, 4096]
+    rng = np.random.default_rng(1024)
+    shapes = [(int(rng.choice(sizes)), int(rng.choice(sizes))) for _ in range(1024)]
+    with hpxfft.Batch([a for a, _ in shapes], [2 * (b // 2 + 1) for _, b in shapes], "f32", "estimate") as bt:
+        arena = torch.zeros(bt.arena_bytes // 4, dtype=torch.float32, device="cuda")
+        src = torch.empty_like(arena)
+        for i, ((r, c), off) in enumerate(zip(shapes, bt.offsets)):
+            g = torch.Generator(device="cuda")
+            g.manual_seed(7919 * i + 1)
+            w = 2 * (c // 2 + 1)
+            src[off // 4: off // 4 + r * w].view(r, w)[:, :c] = torch.rand((r, c), generator=g, device="cuda") * 2 - 1
+        arena.copy_(src)
+        bt.set_stream(stream.cuda_stream)
+        ms = _time_steps(torch, stream, lambda: bt.execute(arena.data_ptr()), steps, warm)
+        bt.synchronize()
+        Bb = bt.measurement("algorithmic_bytes")
+        out["batch_1024_uneven_f32"] = {"ms": ms, "value": Bb / (ms * 1e-3) / 1e9, "unit": "GB/s",
+                                        "frac_of_measured_hbm": Bb / (ms * 1e-3) / 1e9 / peak,
+                                        "instances": 1024, "items": bt.measurement("items"),
+                                        "launches_per_step": 1, "cuda_graph": True,
+                                        "note": "in place, so steps after the first transform the previous output"}
+    del arena, src
+
+    # differentiation: adjoint of the r2c on 64 FP32 2048^2 arrays
+    nb, n = 64, 2048
+    g = torch.Generator(device="cuda")
+    g.manual_seed(64)
+    buf = torch.rand((nb, n, 2 * (n // 2 + 1)), generator=g, device="cuda")
+    with hpxfft.Plan(n, 2 * (n // 2 + 1), nb, "f32", "estimate") as pb:
+        pb.set_stream(stream.cuda_stream)
+        ms = _time_steps(torch, stream, lambda: pb.backward_device(buf.data_ptr()), steps, warm)
+        Bd = nb * algorithmic_bytes(n, n, 4)
+        out["backward_64x2048_f32"] = {"ms": ms, "value": Bd / (ms * 1e-3) / 1e9, "unit": "GB/s",
+                                       "frac_of_measured_hbm": Bd / (ms * 1e-3) / 1e9 / peak}
+    del buf
+    return out
 
 
 def main():

@@ -390,8 +390,11 @@ __device__ __forceinline__ void local_stage(cpx<typename A::T> *s, int L, int lo
     if constexpr (C > 1) crank = cg::this_cluster().block_rank();                         \
     (void)kFixed;
 
-#define HPXFFT_BOUNDS(A, FL) \
-    __launch_bounds__((FL) > 0 ? kFixedThreadsMax : A::kMaxThreads, (FL) > 0 ? kFixedMinBlocks : 1)
+// Compile-time chains: the CTA's own thread count, two CTAs per SM when it
+// has at most 512 threads; runtime plans: the type's maximum, one CTA.
+#define HPXFFT_BOUNDS(A, FL)                                                                     \
+    __launch_bounds__((FL) > 0 ? fixed_threads(FL, FW, A::kEPTFixed) : A::kMaxThreads,           \
+                      (FL) > 0 && fixed_threads(FL, FW, A::kEPTFixed) <= kFixedThreadsMax ? kFixedMinBlocks : 1)
 
 // ------------------------------------------------------------ row r2c kernel
 // Packed-real row transform: z[m] = x[2m] + i x[2m+1], Z = DFT_M(z), then

@@ -19,8 +19,9 @@ struct LaunchShape {
 // for power-of-two sizes: at most 4096 float-float or 8192 FP32 elements per
 // CTA (64 KB of data), the shapes the planner picks.
 // Rows: one row per CTA up to that size (shorter rows packed), longer rows
-// split over a cluster.
-#define HPXFFT_ROW_FIXED_FF(X) X(4096, 0, 1) X(4096, 0, 2) X(4096, 0, 4) X(2048, 1, 1) X(1024, 2, 1) X(512, 3, 1) X(256, 4, 1)
+// split over a cluster; float-float rows of 8192 pairs also run as one
+// 1024-thread CTA (no cluster exchange), which the planner prefers.
+#define HPXFFT_ROW_FIXED_FF(X) X(8192, 0, 1) X(8192, 0, 2) X(4096, 0, 1) X(4096, 0, 2) X(4096, 0, 4) X(2048, 1, 1) X(1024, 2, 1) X(512, 3, 1) X(256, 4, 1)
 #define HPXFFT_ROW_FIXED_F32(X) X(8192, 0, 1) X(8192, 0, 2) X(4096, 1, 1) X(2048, 2, 1) X(1024, 3, 1) X(512, 4, 1)
 // Columns: strips of 4 (float-float) or 8 (FP32) columns, 64-byte row
 // segments; nx >= 2048 splits into local length 1024 over 2..16 CTAs.

