@@ -10,6 +10,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/hpxfft_gb300.h"
@@ -42,7 +43,7 @@ cudaError_t prepare_batch_kernel()
 
 struct Tuning {
     int lag = 8;        // instances whose rows run ahead of their columns
-    int ctas_per_sm = 1;
+    int ctas_per_sm = 2;
 };
 
 // Process-wide cache of tuned batch configurations, keyed by the multiset of
@@ -203,20 +204,43 @@ int hpxfft_batch_create(hpxfft_batch *out, size_t count, const size_t *n_rows, c
     b->real_bytes = precision == HPXFFT_PREC_F32 ? 4 : 8;
     const int maxel = precision == HPXFFT_PREC_F32 ? 8192 : 4096;
     const int cbytes = 2 * (int)b->real_bytes;
-    std::map<std::pair<int, int>, int> dim_index;  // (L, log2W) -> dims
-    std::map<int, int> tw_index;                   // table length -> pool offset
+    std::map<std::tuple<int, int, int>, int> dim_index;  // (kind, L, log2W) -> dims
+    std::map<int, int> tw_index;                         // table length -> pool offset
     int tw_total = 0;
     std::vector<int> row_groups, col_strips;
     size_t off = 0;
-    auto dim_of = [&](int L, int lw) -> int {
-        auto it = dim_index.find({L, lw});
+    auto fixed_id = [&](int kind, int L, int lw) -> int {
+        if (precision != HPXFFT_PREC_F32) return -1;
+#define HPXFFT_X(ID, L_, W_) \
+    if (L == L_ && lw == W_) return ID;
+        if (kind == 0) {
+            HPXFFT_BATCH_ROWS_F32(HPXFFT_X)
+        } else {
+            HPXFFT_BATCH_COLS_F32(HPXFFT_X)
+        }
+#undef HPXFFT_X
+        return -1;
+    };
+    auto dim_of = [&](int kind, int L, int lw) -> int {
+        auto it = dim_index.find({kind, L, lw});
         if (it != dim_index.end()) return it->second;
         BatchDim d{};
         if (!factor_plan(L, d.pp)) return -1;
         d.L = L;
         d.log2W = lw;
+        d.fixed_id = fixed_id(kind, L, lw);
+        d.ptab = 0;
+        if (d.fixed_id >= 0) {
+            // per-pass tables of the compile-time chain (same rule as FixedPasses)
+            d.ptab = tw_total;
+            for (int Ls = 1; Ls < L;) {
+                const int R = fixed_radix(L, Ls, ArithF32::kEPTFixed);
+                if (Ls > 1) tw_total += Ls * (R - 1);
+                Ls *= R;
+            }
+        }
         b->dims.push_back(d);
-        return dim_index[{L, lw}] = (int)b->dims.size() - 1;
+        return dim_index[{kind, L, lw}] = (int)b->dims.size() - 1;
     };
     auto tw_of = [&](int len) {
         auto it = tw_index.find(len);
@@ -245,11 +269,11 @@ int hpxfft_batch_create(hpxfft_batch *out, size_t count, const size_t *n_rows, c
                                  std::to_string(maxel) + ")");
         }
         int rlw = 0;
-        while (rlw < 4 && (in.M << (rlw + 1)) <= maxel && (1 << rlw) < in.nx) ++rlw;
+        while (rlw < 6 && (in.M << (rlw + 1)) <= maxel && (1 << rlw) < in.nx) ++rlw;
         int clw = 6;
         while (clw > 0 && ((in.nx << clw) > maxel || (1 << (clw - 1)) >= in.dcy)) --clw;
-        in.row_dim = dim_of(in.M, rlw);
-        in.col_dim = dim_of(in.nx, clw);
+        in.row_dim = dim_of(0, in.M, rlw);
+        in.col_dim = dim_of(1, in.nx, clw);
         if (in.row_dim < 0 || in.col_dim < 0) {
             delete b;
             return set_error(HPXFFT_ERR_UNSUPPORTED_SIZE,
@@ -309,6 +333,21 @@ int hpxfft_batch_create(hpxfft_batch *out, size_t count, const size_t *n_rows, c
         char *dst = (char *)b->d_tw + (size_t)kv.second * 2 * b->real_bytes;
         e = precision == HPXFFT_PREC_F32 ? TwiddleLaunch<ArithF32>::full(dst, kv.first, b->stream)
                                          : TwiddleLaunch<ArithFF>::full(dst, kv.first, b->stream);
+    }
+    {
+        // per-pass tables of every compile-time dim, at the offsets dim_of took
+        for (auto &d : b->dims) {
+            if (e != cudaSuccess || d.fixed_id < 0) continue;
+            size_t off = (size_t)d.ptab;
+            for (int Ls = 1; Ls < d.L;) {
+                const int R = fixed_radix(d.L, Ls, ArithF32::kEPTFixed);
+                if (Ls > 1) {
+                    e = TwiddleLaunch<ArithF32>::pass((char *)b->d_tw + off * 2 * b->real_bytes, Ls, R, b->stream);
+                    off += (size_t)Ls * (R - 1);
+                }
+                Ls *= R;
+            }
+        }
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess) {

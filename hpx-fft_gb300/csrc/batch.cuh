@@ -21,7 +21,19 @@ struct BatchDim {
     PassPlan pp;
     int L;
     int log2W;
+    int fixed_id;    // index into the compile-time list below, -1: runtime plan
+    int ptab;        // complex entries into the twiddle pool (per-pass tables)
 };
+
+// Compile-time (L, log2 interleave) shapes of the FP32 batch kernel: the
+// lengths 2^k, 3*2^k, 5*2^k between 128 and 4096, each packed to fill a CTA of
+// at most 8192 elements (rows: L = ny/2, columns: L = nx).
+#define HPXFFT_BATCH_ROWS_F32(X) \
+    X(0, 128, 6) X(1, 192, 5) X(2, 256, 5) X(3, 320, 4) X(4, 384, 4) X(5, 512, 4) X(6, 768, 3) X(7, 1024, 3) \
+    X(8, 1280, 2) X(9, 1536, 2) X(10, 2048, 2)
+#define HPXFFT_BATCH_COLS_F32(X) \
+    X(0, 256, 5) X(1, 384, 4) X(2, 512, 4) X(3, 640, 3) X(4, 768, 3) X(5, 1024, 3) X(6, 1536, 2) X(7, 2048, 2) \
+    X(8, 2560, 1) X(9, 3072, 1) X(10, 4096, 1)
 
 struct BatchInst {
     long long offset;  // reals from the arena base
@@ -51,8 +63,23 @@ struct BatchArgs {
 
 constexpr int kBatchThreads = 512;
 
+// One body per compiled shape, not inlined: each gets its own register
+// allocation instead of the union of all of them in the persistent loop.
+template <class A, int FL, int FW>
+__device__ __noinline__ void batch_row(const RowArgs &a, int group)
+{
+    row_r2c_body<A, 1, FL, FW>(a, group, 0);
+}
+template <class A, int FL, int FW>
+__device__ __noinline__ void batch_col(const ColArgs &a, int group)
+{
+    col_body<A, 1, -1, FL, FW>(a, group, 0);
+}
+
+// Two CTAs per SM (64 registers, <= 70 KB shared memory each): while one
+// streams an item in or out, the other computes.
 template <class A>
-__global__ void __launch_bounds__(kBatchThreads, 1) batch_kernel(BatchArgs b)
+__global__ void __launch_bounds__(kBatchThreads, 2) batch_kernel(BatchArgs b)
 {
     using T = typename A::T;
     using S = typename A::S;
@@ -79,7 +106,21 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batch_kernel(BatchArgs b)
             ra.pp = d.pp;
             ra.tw = pool + in.tw_row;
             ra.Ltab = 2 * in.M;
-            row_r2c_body<A, 1, 0, 0>(ra, item.group, 0);
+            ra.ptab = pool + d.ptab;
+            bool done = false;
+            if constexpr (sizeof(S) == 4) {
+                switch (d.fixed_id) {
+#define HPXFFT_X(ID, L_, W_)                                \
+    case ID:                                                \
+        batch_row<A, L_, W_>(ra, item.group);               \
+        done = true;                                        \
+        break;
+                    HPXFFT_BATCH_ROWS_F32(HPXFFT_X)
+#undef HPXFFT_X
+                default: break;
+                }
+            }
+            if (!done) batch_row<A, 0, 0>(ra, item.group);
             __threadfence();
             __syncthreads();
             if (threadIdx.x == 0) atomicAdd(&rows_done[item.inst], 1);
@@ -110,7 +151,21 @@ __global__ void __launch_bounds__(kBatchThreads, 1) batch_kernel(BatchArgs b)
                 ca.pp = d.pp;
                 ca.tw = pool + in.tw_col;
                 ca.Ltab = in.nx;
-                col_body<A, 1, -1, 0, 0>(ca, item.group, 0);
+                ca.ptab = pool + d.ptab;
+                bool done = false;
+                if constexpr (sizeof(S) == 4) {
+                    switch (d.fixed_id) {
+#define HPXFFT_X(ID, L_, W_)                                  \
+    case ID:                                                  \
+        batch_col<A, L_, W_>(ca, item.group);                 \
+        done = true;                                          \
+        break;
+                        HPXFFT_BATCH_COLS_F32(HPXFFT_X)
+#undef HPXFFT_X
+                    default: break;
+                    }
+                }
+                if (!done) batch_col<A, 0, 0>(ca, item.group);
             }
         }
         __syncthreads();  // s_item is rewritten next iteration

@@ -66,9 +66,11 @@ constexpr int kFixedMinBlocks = 2;
 constexpr int kElemsPerThread = 16;
 
 // ----------------------------------------------------------------- storage
-// Data bypasses L1 (loads .cg, stores .cs): each element is read and written
-// once per pass, L1 stays with the twiddles, and a kernel that reads data
-// another SM wrote in the same launch (the batched work queue) sees it at L2.
+// Data loads bypass L1 (.cg), stores stream (.cs): each element is read and
+// written once per pass, L1 stays with the twiddles, and a kernel that reads
+// data another SM wrote in the same launch (the batched work queue) sees it
+// at L2.  (Default-policy stores measured slower on 16384^2 FP32 and no
+// faster on the batch.)
 __device__ __forceinline__ double2 ld_stream(const double *p) { return __ldcg(reinterpret_cast<const double2 *>(p)); }
 __device__ __forceinline__ float2 ld_stream(const float *p) { return __ldcg(reinterpret_cast<const float2 *>(p)); }
 
@@ -201,10 +203,11 @@ __device__ __forceinline__ void fixed_pass(cpx<T> *s, const cpx<T> *__restrict__
     constexpr int NTASK = LR * W;
     constexpr int TPT = (NTASK + NT - 1) / NT;
     cpx<T> v[TPT][R];
+    const bool active = threadIdx.x < NT;  // bodies may run in a larger CTA (batch kernel)
 #pragma unroll
     for (int t = 0; t < TPT; ++t) {
         const int task = threadIdx.x + t * NT;
-        if (NTASK % NT == 0 || task < NTASK) {
+        if (active && (NTASK % NT == 0 || task < NTASK)) {
             const int w = task % W, jj = task / W;
             if constexpr (RAW) {
                 // first pass of the float-float path: the slots still hold the
@@ -240,7 +243,7 @@ __device__ __forceinline__ void fixed_pass(cpx<T> *s, const cpx<T> *__restrict__
 #pragma unroll
     for (int t = 0; t < TPT; ++t) {
         const int task = threadIdx.x + t * NT;
-        if (NTASK % NT == 0 || task < NTASK) {
+        if (active && (NTASK % NT == 0 || task < NTASK)) {
             const int w = task % W, jj = task / W;
             const int k = jj % Ls;
             const int base = (jj - k) * R + k;
@@ -251,7 +254,23 @@ __device__ __forceinline__ void fixed_pass(cpx<T> *s, const cpx<T> *__restrict__
     __syncthreads();
 }
 
-__host__ __device__ constexpr int fixed_radix(int L, int Ls, int maxR) { return (L / Ls) >= maxR ? maxR : L / Ls; }
+// Radix of the pass after Ls: the largest power of two <= maxR dividing the
+// rest, then the odd primes 3, 5, 7, 11, 13.
+__host__ __device__ constexpr int fixed_radix(int L, int Ls, int maxR)
+{
+    const int rest = L / Ls;
+    if (rest % 2 == 0) {
+        int r = 2;
+        while (r * 2 <= maxR && rest % (r * 2) == 0) r *= 2;
+        return r;
+    }
+    if (rest % 3 == 0) return 3;
+    if (rest % 5 == 0) return 5;
+    if (rest % 7 == 0) return 7;
+    if (rest % 11 == 0) return 11;
+    if (rest % 13 == 0) return 13;
+    return rest;
+}
 
 template <class T, int L, int W, int NT, int DIR, int MAXR, int Ls, int Off, bool RAW, bool POST>
 struct FixedPasses {
@@ -280,7 +299,7 @@ __host__ __device__ constexpr int fixed_threads(int L, int log2W, int EPT)
 template <int BATCH, class V, class LD, class USE>
 __device__ __forceinline__ void batched_loop(int nel, int nth, LD ld, USE use)
 {
-    for (int base = threadIdx.x; base < nel; base += BATCH * nth) {
+    for (int base = (int)threadIdx.x < nth ? (int)threadIdx.x : nel; base < nel; base += BATCH * nth) {
         V v[BATCH];
 #pragma unroll
         for (int i = 0; i < BATCH; ++i) {
@@ -386,9 +405,11 @@ __device__ __forceinline__ void local_stage(cpx<typename A::T> *s, int L, int lo
     const int W = 1 << log2W, wmask = W - 1;                                              \
     const int tid = threadIdx.x;                                                          \
     const int nth = kFixed ? fixed_threads(FL, FW, EPT) : (int)blockDim.x;                \
+    const int t0 = tid < nth ? tid : (1 << 30); /* threads past nth idle */               \
     unsigned crank = 0;                                                                   \
     if constexpr (C > 1) crank = cg::this_cluster().block_rank();                         \
-    (void)kFixed;
+    (void)kFixed;                                                                         \
+    (void)t0;
 
 // Compile-time chains: the CTA's own thread count, two CTAs per SM when it
 // has at most 512 threads; runtime plans: the type's maximum, one CTA.
@@ -438,7 +459,7 @@ __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bi
         });
         reduce_exponents<C>(emax, log2W, sE, sEc);
         if constexpr (!kFixed) {
-            for (int t = tid; t < nel; t += nth) {
+            for (int t = t0; t < nel; t += nth) {
                 const double2 v = reinterpret_cast<double2 *>(s)[pidx(t)];
                 const int E = scale_exp(sEc[t & wmask]);
                 s[pidx(t)] = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
@@ -455,7 +476,7 @@ __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bi
 
     if constexpr (C == 1) {
         const int ntask = (M / 2 + 1) << log2W;
-        for (int t = tid; t < ntask; t += nth) {
+        for (int t = t0; t < ntask; t += nth) {
             const int w = t & wmask, k = t >> log2W, row = row0 + w;
             if (row >= a.nrows) continue;
             const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
@@ -493,7 +514,7 @@ __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bi
         }
         cl.sync();
         // my Z[k], k = k20 + (li % Lc) + L * (li / Lc), sit at local index li
-        for (int li = tid; li < L; li += nth) {
+        for (int li = t0; li < L; li += nth) {
             const int k1 = li / Lc, k2 = k20 + li % Lc;
             const int k = k2 + L * k1;
             const int kp = (M - k) % M;
@@ -567,7 +588,7 @@ __global__ void HPXFFT_BOUNDS(A, FL) row_c2r_kernel(RowArgs a)
             });
         reduce_exponents<C>(emax, log2W, sE, sEc);
     }
-    for (int t = tid; t < nel; t += nth) {
+    for (int t = t0; t < nel; t += nth) {
         const int w = t & wmask, m = t >> log2W, row = row0 + w;
         const int k = crank + C * m;
         const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
@@ -597,7 +618,7 @@ __global__ void HPXFFT_BOUNDS(A, FL) row_c2r_kernel(RowArgs a)
     local_stage<A, +1, C, FL, FW, false>(s, L, log2W, a.pp, tw, a.Ltab, ptab, sEc, 2 * (int)crank);
 
     if constexpr (C == 1) {
-        for (int t = tid; t < nel; t += nth) {
+        for (int t = t0; t < nel; t += nth) {
             const int w = t & wmask, m = t >> log2W, row = row0 + w;
             if (row >= a.nrows) continue;
             const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
@@ -612,7 +633,7 @@ __global__ void HPXFFT_BOUNDS(A, FL) row_c2r_kernel(RowArgs a)
         const int E = A::kScaled ? scale_exp(sEc[0]) : 0;
         cl.sync();
         const int Lc = L / C, k20 = crank * Lc;
-        for (int t = tid; t < Lc; t += nth) {
+        for (int t = t0; t < Lc; t += nth) {
             cpx<T> v[C];
 #pragma unroll
             for (int r = 0; r < C; ++r) v[r] = *cl.map_shared_rank(&s[pidx(k20 + t)], r);
@@ -667,7 +688,7 @@ __device__ __forceinline__ void col_body(const ColArgs &a, int strip, int bidx)
         });
         reduce_exponents<C>(emax, log2W, sE, sEc);
         if constexpr (!kFixed) {
-            for (int t = tid; t < nel; t += nth) {
+            for (int t = t0; t < nel; t += nth) {
                 const double2 v = reinterpret_cast<double2 *>(s)[pidx(t)];
                 const int E = scale_exp(sEc[t & wmask]);
                 s[pidx(t)] = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
@@ -681,7 +702,7 @@ __device__ __forceinline__ void col_body(const ColArgs &a, int strip, int bidx)
     local_stage<A, DIR, C, FL, FW, A::kScaled>(s, L, log2W, a.pp, tw, a.Ltab, ptab, sEc, (int)crank);
 
     if constexpr (C == 1) {
-        for (int t = tid; t < nel; t += nth) {
+        for (int t = t0; t < nel; t += nth) {
             const int w = t & wmask, k = t >> log2W, col = col0 + w;
             if (col >= a.ncols) continue;
             const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
@@ -692,7 +713,7 @@ __device__ __forceinline__ void col_body(const ColArgs &a, int strip, int bidx)
         cl.sync();
         const int Lc = L / C, k20 = crank * Lc;
         const int ntask = Lc << log2W;
-        for (int t = tid; t < ntask; t += nth) {
+        for (int t = t0; t < ntask; t += nth) {
             const int w = t & wmask, k2 = k20 + (t >> log2W), col = col0 + w;
             cpx<T> v[C];
 #pragma unroll
@@ -780,7 +801,7 @@ __global__ void HPXFFT_BOUNDS(A, FL) colstep_kernel(ColStepArgs a)
         });
         reduce_exponents<1>(emax, log2W, sE, sEc);
         if constexpr (!kFixed) {
-            for (int t = tid; t < nel; t += nth) {
+            for (int t = t0; t < nel; t += nth) {
                 const double2 v = reinterpret_cast<double2 *>(s)[pidx(t)];
                 const int E = scale_exp(sEc[t & wmask]);
                 s[pidx(t)] = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
@@ -797,7 +818,7 @@ __global__ void HPXFFT_BOUNDS(A, FL) colstep_kernel(ColStepArgs a)
     else
         local_fft<T, DIR>(s, L, log2W, a.pp, tw, a.Ltab);
 
-    for (int t = tid; t < nel; t += nth) {
+    for (int t = t0; t < nel; t += nth) {
         const int w = t & wmask, k = t >> log2W, col = col0 + w;
         if (col >= a.ncols) continue;
         const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
