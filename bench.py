@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--n", type=int, default=16384, help="nx = ny")
     ap.add_argument("--nx", type=int, default=0, help="rows (overrides --n; profiling cases)")
     ap.add_argument("--ny", type=int, default=0, help="columns (overrides --n; profiling cases)")
-    ap.add_argument("--precision", default="f64", choices=["f64", "f32", "f64-native"])
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32", "bf16x3", "f64-native"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP32 / batch / backward sections")
@@ -248,10 +248,11 @@ def run_ours(args):
 
     nx, ny = args.nx, args.ny
     prec = args.precision
-    real_bytes = 4 if prec == "f32" else 8
+    f32 = prec in ("f32", "bf16x3")
+    real_bytes = 4 if f32 else 8
     nc = 2 * (ny // 2 + 1)
     x64 = workload_input(nx, ny, seed=1234 + rank)
-    host = x64.astype(np.float32) if prec == "f32" else x64
+    host = x64.astype(np.float32) if f32 else x64
     dev_in = torch.from_numpy(host).cuda()
     dev_out = torch.empty_like(dev_in)
     stream = torch.cuda.current_stream()
@@ -292,10 +293,10 @@ def run_ours(args):
     # rows of the spectrum are checked through the full-size property
     # (Parseval) and, at rank 0, against the oracle for the whole transform
     out = dev_out.cpu().numpy()
-    spec_out = out.view(np.complex128 if prec != "f32" else np.complex64)
+    spec_out = out.view(np.complex64 if f32 else np.complex128)
 
     # end to end through the host-buffer C ABI call
-    pinned = torch.empty((nx, nc), dtype=torch.float64 if prec != "f32" else torch.float32).pin_memory()
+    pinned = torch.empty((nx, nc), dtype=torch.float32 if f32 else torch.float64).pin_memory()
     host_src = torch.from_numpy(host)
     e2e_times = []
     for i in range(args.e2e_steps + 1):
@@ -312,8 +313,9 @@ def run_ours(args):
     steps = int(plan.measurement("column_steps"))
     kernels = {"row_r2c_kernel": stats["first"]}
     if steps == 2:
-        kernels["colstep_kernel (A)"] = plan.measurement("mean_col_step_a")
-        kernels["colstep_kernel (B)"] = plan.measurement("mean_col_step_b")
+        step_kernel = "colstep_tc_kernel" if prec == "bf16x3" else "colstep_kernel"
+        kernels[f"{step_kernel} (A)"] = plan.measurement("mean_col_step_a")
+        kernels[f"{step_kernel} (B)"] = plan.measurement("mean_col_step_b")
     else:
         kernels["col_kernel"] = stats["second"]
     dominant = max(kernels, key=kernels.get)
@@ -347,12 +349,13 @@ def run_ours(args):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f64" if prec != "f32" else "f32",
+            "dtype": "f32" if f32 else "f64",
             "data": "synthetic: uniform[-1,1) + 4 integer-frequency sinusoids of amplitude 10, seed 1234+rank",
             "config": {
                 "workload": f"2d_r2c_{prec}_{nx}x{ny}",
                 "nx": nx, "ny": ny,
                 "precision": {"f64": "FP64 storage, float-float arithmetic", "f32": "FP32",
+                              "bf16x3": "FP32 storage, split-BF16 tensor-core column stage",
                               "f64-native": "FP64 storage, DFMA arithmetic"}[prec],
                 "layout": "padded vector_2d (n x 2*(n/2+1)), output [kx][ky]",
                 "step": "out-of-place forward transform, input and output resident in HBM",
@@ -421,21 +424,28 @@ def extras(torch, hpxfft, args, x64, oracle_ref, peak):
     nc = 2 * (ny // 2 + 1)
     steps, warm = max(3, args.steps), max(3, args.warmup)
 
-    # precision: FP32 in and out, error against the FP64 oracle
+    # precision: FP32 in and out (CUDA cores, and with the split-BF16 tensor-core
+    # column stage), error against the FP64 oracle
     x32 = torch.from_numpy(x64.astype(np.float32)).cuda()
     y32 = torch.empty_like(x32)
-    with hpxfft.Plan(nx, nc, 1, "f32", "estimate") as p32:
-        p32.set_stream(stream.cuda_stream)
-        ms = _time_steps(torch, stream, lambda: p32.execute_oop(x32.data_ptr(), y32.data_ptr()), steps, warm)
-        B = algorithmic_bytes(nx, ny, 4)
-        sec = {"workload": f"2d_r2c_f32_{nx}x{ny}", "ms": ms, "value": B / (ms * 1e-3) / 1e9, "unit": "GB/s",
-               "frac_of_measured_hbm": B / (ms * 1e-3) / 1e9 / peak}
-        if oracle_ref is not None:
-            got = y32.cpu().numpy().view(np.complex64).astype(np.complex128)
-            d = got - oracle_ref
-            sec["rel_l2_vs_fp64_oracle"] = float(np.linalg.norm(d.ravel()) / np.linalg.norm(oracle_ref.ravel()))
-            sec["max_abs_err_vs_fp64_oracle"] = float(np.abs(d).max())
-        out["precision_f32"] = sec
+    for prec in ("f32", "bf16x3"):
+        if prec == "bf16x3" and (nx < 1024 or nx > 65536 or nx & (nx - 1)):
+            continue
+        with hpxfft.Plan(nx, nc, 1, prec, "estimate") as p32:
+            p32.set_stream(stream.cuda_stream)
+            ms = _time_steps(torch, stream, lambda: p32.execute_oop(x32.data_ptr(), y32.data_ptr()), steps, warm)
+            p32.synchronize()
+            B = algorithmic_bytes(nx, ny, 4)
+            sec = {"workload": f"2d_r2c_{prec}_{nx}x{ny}", "ms": ms, "value": B / (ms * 1e-3) / 1e9, "unit": "GB/s",
+                   "frac_of_measured_hbm": B / (ms * 1e-3) / 1e9 / peak}
+            if prec == "bf16x3":
+                sec["tensor_core_stage"] = "first radix-16 pass of both column steps, tcgen05 kind::f16, 3-term BF16 split"
+            if oracle_ref is not None:
+                got = y32.cpu().numpy().view(np.complex64).astype(np.complex128)
+                d = got - oracle_ref
+                sec["rel_l2_vs_fp64_oracle"] = float(np.linalg.norm(d.ravel()) / np.linalg.norm(oracle_ref.ravel()))
+                sec["max_abs_err_vs_fp64_oracle"] = float(np.abs(d).max())
+            out[f"precision_{prec}"] = sec
     del x32, y32
 
     # batching: 1024 uneven FP32 instances

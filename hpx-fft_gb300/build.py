@@ -30,6 +30,7 @@ SOURCES = [
     "kernels_f32_rows.cu",
     "kernels_f32_cols.cu",
     "kernels_f64.cu",
+    "kernels_tc_cols.cu",
     "twiddles.cu",
     "plan.cu",
     "batch.cu",

@@ -57,6 +57,19 @@ struct ColStepLaunch {
     static cudaError_t run(const ColStepArgs &a, int dir, const LaunchShape &s, int FL, cudaStream_t st);
 };
 
+// Split-BF16 tensor-core column steps (kernels_tc_cols.cu): lengths 16 * L2,
+// L2 in {2, 4, 8, 16}, 512 length-16 vectors (8192 elements) per CTA.
+struct TcColStepLaunch {
+    static cudaError_t prepare();
+    static bool supports(int L);
+    static int log2W(int L);  // columns per CTA: 8192 / L
+    static int threads();
+    static size_t smem();
+    static size_t table_bytes();
+    static cudaError_t table(void *dft, cudaStream_t st);
+    static cudaError_t run(const ColStepArgs &a, const void *dft, int *error, int dir, dim3 grid, cudaStream_t st);
+};
+
 template <class A>
 struct TwiddleLaunch {
     static cudaError_t full(void *tab, int n, cudaStream_t st);

@@ -62,6 +62,10 @@ struct hpxfft_plan_s {
     int N1 = 0, N2 = 0;
     hpxfft_gpu::DimPlan colA, colB;
     void *scratch = nullptr;
+    // split-BF16 precision: both column steps on the tensor cores
+    bool tc_cols = false;
+    void *tc_dft = nullptr;     // BF16 DFT-16 matrix splits
+    int *dev_error = nullptr;   // set by a tensor-core kernel whose wait gave up
     void *tw_row = nullptr, *tw_col = nullptr;
     void *dbuf = nullptr;
     size_t dbuf_bytes = 0;
@@ -105,7 +109,11 @@ static bool factorize(int L, int max_radix, PassPlan &pp)
 
 // Elements of one CTA's transform(s): 4096 float-float (or FP64) pairs or
 // 8192 FP32 pairs, 64 KB of data, so two CTAs share an SM.
-static int max_elems_for(int prec) { return prec == HPXFFT_PREC_F32 ? 8192 : 4096; }
+// FP32 storage: the FP32 path and the split-BF16 path (FP32 outside the
+// tensor-core stage)
+static bool f32_storage(int prec) { return prec == HPXFFT_PREC_F32 || prec == HPXFFT_PREC_BF16X3; }
+
+static int max_elems_for(int prec) { return f32_storage(prec) ? 8192 : 4096; }
 
 static int threads_for(int nel)
 {
@@ -154,7 +162,7 @@ static bool plan_cols(hpxfft_plan_s &p)
 {
     const int maxel = max_elems_for(p.prec);
     const size_t cbytes = 2 * p.real_bytes;
-    int pref = p.prec == HPXFFT_PREC_F32 ? 3 : 2;
+    int pref = f32_storage(p.prec) ? 3 : 2;
     while (pref > 0 && ((size_t)1 << (pref - 1)) >= p.dcy) --pref;
     for (int log2W = pref; log2W >= 0; --log2W) {
         for (int C : {1, 2, 4, 8, 16}) {
@@ -193,6 +201,24 @@ static bool plan_colsteps(hpxfft_plan_s &p)
     p.N1 = (int)(p.nx / p.N2);
     const int maxel = max_elems_for(p.prec);
     const size_t cbytes = 2 * p.real_bytes;
+    if (p.prec == HPXFFT_PREC_BF16X3) {
+        // tensor-core steps: 8192 elements per CTA, 8192 / L columns
+        for (int step = 0; step < 2; ++step) {
+            DimPlan &d = step == 0 ? p.colA : p.colB;
+            const int L = step == 0 ? p.N2 : p.N1;
+            if (!TcColStepLaunch::supports(L) || !factorize(L, 16, d.pp)) return false;
+            d.C = 1;
+            d.L = L;
+            d.log2W = TcColStepLaunch::log2W(L);
+            d.shape.threads = TcColStepLaunch::threads();
+            d.shape.smem = TcColStepLaunch::smem();
+            d.shape.cluster = 1;
+            const size_t strips = (p.dcy + ((size_t)1 << d.log2W) - 1) >> d.log2W;
+            const size_t groups = step == 0 ? (size_t)p.N1 : (size_t)p.N2;
+            d.shape.grid = dim3((unsigned)(groups * strips), (unsigned)p.batch, 1);
+        }
+        return true;
+    }
     int wcap = 6;  // at most 64 columns per strip
     while (wcap > 0 && ((size_t)1 << (wcap - 1)) >= p.dcy) --wcap;
     for (int step = 0; step < 2; ++step) {
@@ -243,6 +269,7 @@ static bool has_fixed_step(int prec, const DimPlan &d)
     switch (prec) {
     case HPXFFT_PREC_F64: return ColStepLaunch<ArithFF>::has_fixed(d.L, d.log2W);
     case HPXFFT_PREC_F32: return ColStepLaunch<ArithF32>::has_fixed(d.L, d.log2W);
+    case HPXFFT_PREC_BF16X3: return TcColStepLaunch::supports(d.L);  // FP32 chain after the tensor-core pass
     default: return false;
     }
 }
@@ -253,6 +280,7 @@ static bool has_fixed(int prec, bool rows, const DimPlan &d)
     case HPXFFT_PREC_F64:
         return rows ? RowLaunch<ArithFF>::has_fixed(d.L, d.log2W, d.C) : ColLaunch<ArithFF>::has_fixed(d.L, d.log2W, d.C);
     case HPXFFT_PREC_F32:
+    case HPXFFT_PREC_BF16X3:
         return rows ? RowLaunch<ArithF32>::has_fixed(d.L, d.log2W, d.C)
                     : ColLaunch<ArithF32>::has_fixed(d.L, d.log2W, d.C);
     default: return false;
@@ -260,7 +288,7 @@ static bool has_fixed(int prec, bool rows, const DimPlan &d)
 }
 
 // elements per thread (= largest radix) of the compile-time chains
-static int fixed_ept(int prec) { return prec == HPXFFT_PREC_F32 ? ArithF32::kEPTFixed : ArithFF::kEPTFixed; }
+static int fixed_ept(int prec) { return f32_storage(prec) ? ArithF32::kEPTFixed : ArithFF::kEPTFixed; }
 
 // (Ls, R) of every pass of the compile-time chain for length L, in order
 // (the same rule as FixedPasses: the largest radix, then the remainder)
@@ -275,11 +303,30 @@ static std::vector<std::pair<int, int>> fixed_chain(int L, int maxR)
     return v;
 }
 
+static cudaError_t prepare_tc_once()
+{
+    static std::mutex mu;
+    static bool done[kMaxDevices] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done[dev]) return cudaSuccess;
+    e = TcColStepLaunch::prepare();
+    if (e == cudaSuccess) done[dev] = true;
+    return e;
+}
+
 static cudaError_t prepare_prec(int prec)
 {
     switch (prec) {
     case HPXFFT_PREC_F64: return prepare_once<ArithFF>();
     case HPXFFT_PREC_F64_NATIVE: return prepare_once<ArithF64>();
+    case HPXFFT_PREC_BF16X3: {
+        cudaError_t e = prepare_once<ArithF32>();
+        return e == cudaSuccess ? prepare_tc_once() : e;
+    }
     default: return prepare_once<ArithF32>();
     }
 }
@@ -323,7 +370,7 @@ static int setup_fixed(hpxfft_plan_s &p, DimPlan &d, bool rows, cudaStream_t st,
         off += (size_t)c.first * (c.second - 1);
     }
     d.FL = d.L;
-    d.shape.threads = fixed_threads(d.L, d.log2W, fixed_ept(p.prec));
+    if (!(step && p.prec == HPXFFT_PREC_BF16X3)) d.shape.threads = fixed_threads(d.L, d.log2W, fixed_ept(p.prec));
     return HPXFFT_OK;
 }
 
@@ -412,6 +459,14 @@ template <class A>
 static cudaError_t run_columns(hpxfft_plan_s &p, void *data, int dir)
 {
     if (!p.col_two_step) return ColLaunch<A>::run(col_args(p, data), dir, p.col.shape, p.col.FL, p.stream);
+    if (p.tc_cols) {
+        cudaError_t e = TcColStepLaunch::run(colstep_args(p, 0, data, p.scratch), p.tc_dft, p.dev_error, dir,
+                                             p.colA.shape.grid, p.stream);
+        if (e != cudaSuccess) return e;
+        if ((e = cudaEventRecord(p.kev[p.next % hpxfft_plan_s::kSlots][3], p.stream)) != cudaSuccess) return e;
+        return TcColStepLaunch::run(colstep_args(p, 1, p.scratch, data), p.tc_dft, p.dev_error, dir,
+                                    p.colB.shape.grid, p.stream);
+    }
     cudaError_t e = ColStepLaunch<A>::run(colstep_args(p, 0, data, p.scratch), dir, p.colA.shape, p.colA.FL, p.stream);
     if (e != cudaSuccess) return e;
     if ((e = cudaEventRecord(p.kev[p.next % hpxfft_plan_s::kSlots][3], p.stream)) != cudaSuccess) return e;
@@ -527,7 +582,10 @@ static std::string describe(const hpxfft_plan_s &p, const DimPlan &d, const char
              "precision=%s)",
              what, len, d.C, d.L, radices.c_str(), d.FL ? "compile-time" : "runtime", 1 << d.log2W, d.shape.grid.x,
              d.shape.grid.y, d.shape.threads, d.shape.smem,
-             p.prec == HPXFFT_PREC_F64 ? "f64-floatfloat" : (p.prec == HPXFFT_PREC_F64_NATIVE ? "f64-dfma" : "f32"));
+             p.prec == HPXFFT_PREC_F64          ? "f64-floatfloat"
+             : p.prec == HPXFFT_PREC_F64_NATIVE ? "f64-dfma"
+             : p.prec == HPXFFT_PREC_BF16X3     ? (p.tc_cols && &d != &p.row ? "bf16x3-tcgen05" : "f32")
+                                                : "f32");
     return buf;
 }
 
@@ -562,7 +620,7 @@ int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
     if (!out) return fail(HPXFFT_ERR_INVALID_ARG, "plan pointer is null");
     *out = nullptr;
     if (!valid_flag(plan_flag)) return fail(HPXFFT_ERR_INVALID_ARG, "Invalid FFTW plan flag string");
-    if (precision < HPXFFT_PREC_F64 || precision > HPXFFT_PREC_F32)
+    if (precision < HPXFFT_PREC_F64 || precision > HPXFFT_PREC_BF16X3)
         return fail(HPXFFT_ERR_INVALID_ARG, "unknown precision");
     if (n_row == 0 || batch == 0) return fail(HPXFFT_ERR_INVALID_ARG, "empty array");
     if (n_col < 4 || n_col % 2) return fail(HPXFFT_ERR_UNSUPPORTED_SIZE, "n_col must be 2*(ny/2+1) with ny >= 2 even");
@@ -579,8 +637,8 @@ int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
     p->batch = batch;
     p->prec = precision;
     p->flag = plan_flag;
-    p->real_bytes = precision == HPXFFT_PREC_F32 ? 4 : 8;
-    p->tw_elem = precision == HPXFFT_PREC_F32 ? 8 : 16;
+    p->real_bytes = f32_storage(precision) ? 4 : 8;
+    p->tw_elem = f32_storage(precision) ? 8 : 16;
     if (!plan_rows(*p) || !plan_cols(*p)) {
         delete p;
         return fail(HPXFFT_ERR_UNSUPPORTED_SIZE,
@@ -621,6 +679,27 @@ int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
     bool want_steps = p->col.C >= 8;
     if (force && !strcmp(force, "cluster")) want_steps = false;
     if (force && !strcmp(force, "steps")) want_steps = true;
+    if (precision == HPXFFT_PREC_BF16X3) {
+        // the tensor-core stage lives in the column steps: nx = N1 * N2 with
+        // N1, N2 in {32, 64, 128, 256}
+        if (rc == HPXFFT_OK && !plan_colsteps(*p)) {
+            hpxfft_plan_destroy(p);
+            return fail(HPXFFT_ERR_UNSUPPORTED_SIZE, "split-BF16 precision needs n_row a power of two in [1024, 65536]");
+        }
+        want_steps = true;
+        if (rc == HPXFFT_OK) {
+            if (cudaMalloc(&p->tc_dft, TcColStepLaunch::table_bytes()) != cudaSuccess ||
+                cudaMalloc(&p->dev_error, sizeof(int)) != cudaSuccess) {
+                cudaGetLastError();
+                rc = fail(HPXFFT_ERR_ALLOC, "tensor-core tables");
+            } else if ((e = TcColStepLaunch::table(p->tc_dft, p->stream)) != cudaSuccess ||
+                       (e = cudaMemsetAsync(p->dev_error, 0, sizeof(int), p->stream)) != cudaSuccess) {
+                rc = cuda_fail(e, "tensor-core tables");
+            } else {
+                p->tc_cols = true;
+            }
+        }
+    }
     if (rc == HPXFFT_OK && precision != HPXFFT_PREC_F64_NATIVE && want_steps && plan_colsteps(*p)) {
         rc = setup_fixed(*p, p->colA, false, p->stream, 1);
         if (rc == HPXFFT_OK) rc = setup_fixed(*p, p->colB, false, p->stream, 2);
@@ -668,6 +747,8 @@ int hpxfft_plan_destroy(hpxfft_plan p)
     cudaFree(p->colB.ptab);
     cudaFree(p->scratch);
     cudaFree(p->dbuf);
+    cudaFree(p->tc_dft);
+    cudaFree(p->dev_error);
     for (auto &slot : p->kev)
         for (auto &ev : slot)
             if (ev) cudaEventDestroy(ev);
@@ -725,6 +806,19 @@ static int ensure_dbuf(hpxfft_plan p)
     return HPXFFT_OK;
 }
 
+// HPXFFT_ERR_TIMEOUT (and clears the flag) when a tensor-core kernel's wait gave up
+static int check_device_error(hpxfft_plan p)
+{
+    if (!p->dev_error) return HPXFFT_OK;
+    int flag = 0;
+    cudaError_t e = cudaMemcpyAsync(&flag, p->dev_error, sizeof(int), cudaMemcpyDeviceToHost, p->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "error flag");
+    if (!flag) return HPXFFT_OK;
+    cudaMemsetAsync(p->dev_error, 0, sizeof(int), p->stream);
+    return fail(HPXFFT_ERR_TIMEOUT, "tensor-core MMA completion wait timed out");
+}
+
 int hpxfft_execute_r2c_host(hpxfft_plan p, void *h)
 {
     if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
@@ -743,7 +837,16 @@ int hpxfft_execute_r2c_host(hpxfft_plan p, void *h)
     if ((e = cudaEventRecord(p->ev_copy[1], p->stream)) != cudaSuccess) return cuda_fail(e, "event");
     if ((e = cudaEventSynchronize(p->ev_copy[1])) != cudaSuccess) return cuda_fail(e, "transform");
     p->pending_copy = true;
-    return collect(*p);
+    if ((rc = collect(*p)) != HPXFFT_OK) return rc;
+    return check_device_error(p);
+}
+
+int hpxfft_plan_synchronize(hpxfft_plan p)
+{
+    if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
+    cudaError_t e = cudaStreamSynchronize(p->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "transform");
+    return check_device_error(p);
 }
 
 int hpxfft_execute_c2r(hpxfft_plan p, void *d)

@@ -23,6 +23,7 @@ HPXFFT_ERR_IO = 7
 PREC_F64 = 0
 PREC_F64_NATIVE = 1
 PREC_F32 = 2
+PREC_BF16X3 = 3
 
 # every symbol the header declares: name -> (restype, argtypes)
 _vp = ctypes.c_void_p
@@ -56,6 +57,7 @@ SIGNATURES = {
     "hpxfft_batch_set_stream": (_ci, [_vp, _vp]),
     "hpxfft_batch_execute": (_ci, [_vp, _vp]),
     "hpxfft_batch_synchronize": (_ci, [_vp]),
+    "hpxfft_plan_synchronize": (_ci, [_vp]),
     "hpxfft_batch_get_measurement": (_ci, [_vp, _cs, ctypes.POINTER(ctypes.c_double)]),
     "hpxfft_wisdom_export": (_ci, [_cs]),
     "hpxfft_wisdom_import": (_ci, [_cs]),

@@ -11,6 +11,7 @@ _PRECISIONS = {
     "f64": _capi.PREC_F64,
     "f64-native": _capi.PREC_F64_NATIVE,
     "f32": _capi.PREC_F32,
+    "bf16x3": _capi.PREC_BF16X3,
 }
 
 
@@ -24,7 +25,8 @@ def precision_code(precision) -> int:
 
 
 def real_dtype(precision) -> np.dtype:
-    return np.dtype(np.float32) if precision_code(precision) == _capi.PREC_F32 else np.dtype(np.float64)
+    f32 = precision_code(precision) in (_capi.PREC_F32, _capi.PREC_BF16X3)
+    return np.dtype(np.float32) if f32 else np.dtype(np.float64)
 
 
 class Plan:
@@ -82,6 +84,10 @@ class Plan:
 
     def backward_device(self, ptr: int) -> None:
         _capi.check(self._lib.hpxfft_execute_r2c_backward(self.handle, ctypes.c_void_p(ptr)))
+
+    def synchronize(self) -> None:
+        """Wait for the plan's stream; raises on a timed-out tensor-core wait."""
+        _capi.check(self._lib.hpxfft_plan_synchronize(self.handle))
 
     def execute_host(self, values: np.ndarray) -> np.ndarray:
         """In-place forward transform of a host array (copy in, transform, copy out)."""

@@ -17,7 +17,10 @@
  * Precision: HPXFFT_PREC_F64 stores doubles and computes in float-float on
  * the FP32 pipes (about 48 significant bits; relative L2 error vs FP64 FFTW
  * is ~1e-14); HPXFFT_PREC_F64_NATIVE computes with DFMA (slow on GB300,
- * kept as a cross-check); HPXFFT_PREC_F32 stores and computes float.
+ * kept as a cross-check); HPXFFT_PREC_F32 stores and computes float;
+ * HPXFFT_PREC_BF16X3 stores float and runs the first radix-16 stage of each
+ * column DFT as a dense complex matmul on the tensor cores (tcgen05, BF16
+ * operands split three ways, FP32 accumulation), the other stages in FP32.
  */
 #ifndef HPXFFT_GB300_H
 #define HPXFFT_GB300_H
@@ -48,7 +51,8 @@ typedef enum {
 typedef enum {
     HPXFFT_PREC_F64 = 0,        /* FP64 in HBM, float-float arithmetic */
     HPXFFT_PREC_F64_NATIVE = 1, /* FP64 in HBM, DFMA arithmetic */
-    HPXFFT_PREC_F32 = 2         /* FP32 in HBM and arithmetic */
+    HPXFFT_PREC_F32 = 2,        /* FP32 in HBM and arithmetic */
+    HPXFFT_PREC_BF16X3 = 3      /* FP32 in HBM; split-BF16 tensor-core column stage; n_row a power of two, 1024..65536 */
 } hpxfft_precision;
 
 typedef struct hpxfft_plan_s *hpxfft_plan;
@@ -102,6 +106,12 @@ HPXFFT_API int hpxfft_execute_c2r(hpxfft_plan plan, void *device_values);
  * dL/dRe X + i dL/dIm X over the half spectrum and receives dL/dx (pads 0).
  * No reference counterpart (gradient for fft_2d_r2c_backward). */
 HPXFFT_API int hpxfft_execute_r2c_backward(hpxfft_plan plan, void *device_values);
+
+/* Wait for every transform issued on the plan's stream; HPXFFT_ERR_TIMEOUT
+ * if a bounded device-side wait of a tensor-core kernel gave up (the flag is
+ * cleared by the call).  No reference counterpart (FFTW calls return when
+ * done). */
+HPXFFT_API int hpxfft_plan_synchronize(hpxfft_plan plan);
 
 /* Measurement by key, seconds unless stated: "total", "first_fftw" (row
  * kernel), "first_trans" (0: fused), "second_fftw" (column kernel),
