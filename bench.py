@@ -307,6 +307,7 @@ def run_ours(args):
     e2e_s = sum(e2e_times) / len(e2e_times)
     h2d = plan.measurement("h2d")
     d2h = plan.measurement("d2h")
+    zero_copy = plan.measurement("host_zero_copy") == 1.0
 
     peak, peak_kind = measured_peak_hbm()
     # per launch: every kernel of the step reads S and writes S (B / 2)
@@ -319,6 +320,7 @@ def run_ours(args):
     else:
         kernels["col_kernel"] = stats["second"]
     dominant = max(kernels, key=kernels.get)
+    traffic = profiled_traffic(prec, nx, ny, dominant)
     dom_t = kernels[dominant]
     per_kernel_bytes = B / 2.0
     achieved = per_kernel_bytes / dom_t / 1e9 if dom_t > 0 else 0.0
@@ -359,7 +361,8 @@ def run_ours(args):
                               "f64-native": "FP64 storage, DFMA arithmetic"}[prec],
                 "layout": "padded vector_2d (n x 2*(n/2+1)), output [kx][ky]",
                 "step": "out-of-place forward transform, input and output resident in HBM",
-                "l2": "no flush: input and output are 2.1 GB each, far above the 129 MB L2",
+                "l2": ("no flush: input and output are %.2f GB each, above the 129 MB L2" % (nx * nc * real_bytes / 1e9)
+                       if nx * nc * real_bytes > 129e6 else "no flush: arrays smaller than L2, numbers are L2-warm"),
                 "parallelism": "replicas" if world > 1 else "single GPU",
                 "rel_l2_vs_oracle": rel,
             },
@@ -373,7 +376,9 @@ def run_ours(args):
                 "peak_kind": peak_kind,
                 "unit": "GB/s",
                 "frac": achieved / peak,
-                "traffic": None,
+                "traffic": traffic,
+                "traffic_source": "profiles/dram_traffic_%s_%d.md (ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                  "scaled to a full launch)" % (prec, nx) if traffic else None,
                 "algorithmic_bytes_per_launch": per_kernel_bytes,
             },
             "e2e": {
@@ -384,6 +389,8 @@ def run_ours(args):
                 "ms_per_step": 1e3 * e2e_s,
                 "h2d_ms": 1e3 * h2d,
                 "d2h_ms": 1e3 * d2h,
+                "host_path": ("zero-copy: the row pass reads and the last column step writes the page-locked host "
+                              "buffer over the host link" if zero_copy else "staged through a device buffer"),
             },
             "clocks": clk.summary(),
         }
@@ -411,6 +418,29 @@ def _time_steps(torch, stream, fn, steps, warmup):
     e1.record(stream)
     torch.cuda.synchronize()
     return e0.elapsed_time(e1) / steps
+
+
+def profiled_traffic(prec, nx, ny, label):
+    """DRAM bytes per launch of kernel `label` from the committed ncu summary
+    for this precision and size (None when there is none)."""
+    if nx != ny:
+        return None
+    path = os.path.join(REPO, "profiles", f"dram_traffic_{prec}_{nx}.md")
+    if not os.path.exists(path):
+        return None
+    name = label.split(" ")[0]
+    step = {"(A)": "(step A)", "(B)": "(step B)"}.get(label.split(" ")[-1]) if " " in label else None
+    for line in open(path):
+        cells = [c.strip() for c in line.strip().strip("|").split("|")]
+        if len(cells) < 8 or not cells[0].startswith("`" + name):
+            continue
+        if step and step not in cells[0]:
+            continue
+        try:
+            return float(cells[6])
+        except ValueError:
+            return None
+    return None
 
 
 def extras(torch, hpxfft, args, x64, oracle_ref, peak):

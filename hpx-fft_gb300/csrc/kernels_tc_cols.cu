@@ -5,6 +5,7 @@
 namespace hpxfft_gpu {
 
 #define HPXFFT_TC_LENGTHS(X) X(32) X(64) X(128) X(256)
+#define HPXFFT_TC_SHAPES(X) X(32, 512) X(64, 512) X(128, 512) X(256, 512) X(32, 256) X(64, 256) X(128, 256) X(256, 256)
 
 // polls of the MMA completion barrier before a CTA reports a timeout
 constexpr long long kTcSpinLimit = 1LL << 22;
@@ -12,14 +13,14 @@ constexpr long long kTcSpinLimit = 1LL << 22;
 cudaError_t TcColStepLaunch::prepare()
 {
     cudaError_t e = cudaSuccess;
-#define HPXFFT_X(L)                                                                                              \
-    if ((e = cudaFuncSetAttribute(colstep_tc_kernel<-1, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,         \
-                                  (int)kTcSmem)) != cudaSuccess)                                                  \
+#define HPXFFT_X(L, NV)                                                                                          \
+    if ((e = cudaFuncSetAttribute(colstep_tc_kernel<-1, L, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize,     \
+                                  (int)tc_smem(NV))) != cudaSuccess)                                              \
         return e;                                                                                                \
-    if ((e = cudaFuncSetAttribute(colstep_tc_kernel<+1, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,         \
-                                  (int)kTcSmem)) != cudaSuccess)                                                  \
+    if ((e = cudaFuncSetAttribute(colstep_tc_kernel<+1, L, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize,     \
+                                  (int)tc_smem(NV))) != cudaSuccess)                                              \
         return e;
-    HPXFFT_TC_LENGTHS(HPXFFT_X)
+    HPXFFT_TC_SHAPES(HPXFFT_X)
 #undef HPXFFT_X
     return e;
 }
@@ -33,9 +34,9 @@ bool TcColStepLaunch::supports(int L)
     return false;
 }
 
-int TcColStepLaunch::log2W(int L) { return ilog2c(kTcVectors / (L / 16)); }
-int TcColStepLaunch::threads() { return kTcThreads; }
-size_t TcColStepLaunch::smem() { return kTcSmem; }
+int TcColStepLaunch::log2W(int L, int nv) { return ilog2c(nv / (L / 16)); }
+int TcColStepLaunch::threads(int nv) { return nv; }
+size_t TcColStepLaunch::smem(int nv) { return tc_smem(nv); }
 size_t TcColStepLaunch::table_bytes() { return 2 * (size_t)kTcBBytes; }
 
 cudaError_t TcColStepLaunch::table(void *dft, cudaStream_t st)
@@ -52,16 +53,15 @@ cudaError_t TcColStepLaunch::run(const ColStepArgs &a, const void *dft, int *err
     ta.dft = dft;
     ta.error = error;
     ta.spin_limit = kTcSpinLimit;
-#define HPXFFT_X(L_)                                                                                   \
-    if (a.L == L_) {                                                                                   \
-        if (a.log2W != log2W(L_)) return cudaErrorInvalidValue;                                        \
+#define HPXFFT_X(L_, NV)                                                                               \
+    if (a.L == L_ && a.log2W == log2W(L_, NV)) {                                                       \
         if (dir < 0)                                                                                   \
-            colstep_tc_kernel<-1, L_><<<grid, kTcThreads, kTcSmem, st>>>(ta);                          \
+            colstep_tc_kernel<-1, L_, NV><<<grid, NV, tc_smem(NV), st>>>(ta);                          \
         else                                                                                           \
-            colstep_tc_kernel<+1, L_><<<grid, kTcThreads, kTcSmem, st>>>(ta);                          \
+            colstep_tc_kernel<+1, L_, NV><<<grid, NV, tc_smem(NV), st>>>(ta);                          \
         return cudaGetLastError();                                                                     \
     }
-    HPXFFT_TC_LENGTHS(HPXFFT_X)
+    HPXFFT_TC_SHAPES(HPXFFT_X)
 #undef HPXFFT_X
     return cudaErrorInvalidValue;
 }

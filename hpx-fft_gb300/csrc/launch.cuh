@@ -21,12 +21,12 @@ struct LaunchShape {
 // Rows: one row per CTA up to that size (shorter rows packed), longer rows
 // split over a cluster; float-float rows of 8192 pairs also run as one
 // 1024-thread CTA (no cluster exchange), which the planner prefers.
-#define HPXFFT_ROW_FIXED_FF(X) X(8192, 0, 1) X(8192, 0, 2) X(4096, 0, 1) X(4096, 0, 2) X(4096, 0, 4) X(2048, 1, 1) X(1024, 2, 1) X(512, 3, 1) X(256, 4, 1)
-#define HPXFFT_ROW_FIXED_F32(X) X(8192, 0, 1) X(8192, 0, 2) X(4096, 1, 1) X(2048, 2, 1) X(1024, 3, 1) X(512, 4, 1)
+#define HPXFFT_ROW_FIXED_FF(X) X(8192, 0, 1) X(8192, 0, 2) X(4096, 0, 1) X(4096, 0, 2) X(4096, 0, 4) X(2048, 1, 1) X(1024, 2, 1) X(512, 3, 1) X(256, 4, 1) X(128, 4, 1)
+#define HPXFFT_ROW_FIXED_F32(X) X(8192, 0, 1) X(8192, 0, 2) X(4096, 1, 1) X(2048, 2, 1) X(1024, 3, 1) X(512, 4, 1) X(256, 4, 1) X(128, 4, 1)
 // Columns: strips of 4 (float-float) or 8 (FP32) columns, 64-byte row
 // segments; nx >= 2048 splits into local length 1024 over 2..16 CTAs.
 #define HPXFFT_COL_FIXED_FF(X) X(256, 2, 1) X(512, 2, 1) X(1024, 2, 1) X(1024, 2, 2) X(1024, 2, 4) X(1024, 2, 8) X(1024, 2, 16) X(2048, 1, 16)
-#define HPXFFT_COL_FIXED_F32(X) X(512, 3, 1) X(1024, 3, 1) X(1024, 3, 2) X(1024, 3, 4) X(1024, 3, 8) X(1024, 3, 16) X(2048, 2, 16)
+#define HPXFFT_COL_FIXED_F32(X) X(256, 3, 1) X(512, 3, 1) X(1024, 3, 1) X(1024, 3, 2) X(1024, 3, 4) X(1024, 3, 8) X(1024, 3, 16) X(2048, 2, 16)
 
 template <class A>
 struct RowLaunch {
@@ -58,13 +58,13 @@ struct ColStepLaunch {
 };
 
 // Split-BF16 tensor-core column steps (kernels_tc_cols.cu): lengths 16 * L2,
-// L2 in {2, 4, 8, 16}, 512 length-16 vectors (8192 elements) per CTA.
+// L2 in {2, 4, 8, 16}, nv = 512 or 256 length-16 vectors per CTA.
 struct TcColStepLaunch {
     static cudaError_t prepare();
     static bool supports(int L);
-    static int log2W(int L);  // columns per CTA: 8192 / L
-    static int threads();
-    static size_t smem();
+    static int log2W(int L, int nv);  // columns per CTA: 16 nv / L
+    static int threads(int nv);
+    static size_t smem(int nv);
     static size_t table_bytes();
     static cudaError_t table(void *dft, cudaStream_t st);
     static cudaError_t run(const ColStepArgs &a, const void *dft, int *error, int dir, dim3 grid, cudaStream_t st);

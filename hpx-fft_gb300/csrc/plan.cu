@@ -77,6 +77,7 @@ struct hpxfft_plan_s {
     long long next = 0, done = 0;
     cudaEvent_t ev_copy[2] = {};  // before the host->device copy, after the device->host copy
     bool pending_copy = false;
+    bool last_zero_copy = false;  // the last host-buffer transform read and wrote host memory directly
     double sum_first = 0, sum_second = 0, sum_total = 0, sum_step_a = 0;
     long long nsum = 0;
     std::map<std::string, double> meas;
@@ -127,8 +128,10 @@ static int threads_for(int nel)
 static bool plan_rows(hpxfft_plan_s &p)
 {
     // float-float rows of 8192 pairs fit one 1024-thread CTA: faster than a
-    // 2-CTA cluster split (measured on 16384^2: 4.3 vs 5.1 ms)
+    // 2-CTA cluster split (measured on 16384^2: 4.3 vs 5.1 ms); shorter rows
+    // are packed only up to the compiled 4096-pair shapes
     const int maxel = p.prec == HPXFFT_PREC_F64 ? 8192 : max_elems_for(p.prec);
+    const int packel = max_elems_for(p.prec);
     const size_t cbytes = 2 * p.real_bytes;
     for (int C : {1, 2, 4}) {
         if (p.M % C) continue;
@@ -139,7 +142,7 @@ static bool plan_rows(hpxfft_plan_s &p)
         if (!factorize(L, 16, pp)) return false;
         int log2W = 0;
         if (C == 1)
-            while (log2W < 4 && (L << (log2W + 1)) <= maxel && ((size_t)1 << log2W) < p.nx) ++log2W;
+            while (log2W < 4 && (L << (log2W + 1)) <= packel && ((size_t)1 << log2W) < p.nx) ++log2W;
         DimPlan &d = p.row;
         d.C = C;
         d.L = L;
@@ -202,16 +205,21 @@ static bool plan_colsteps(hpxfft_plan_s &p)
     const int maxel = max_elems_for(p.prec);
     const size_t cbytes = 2 * p.real_bytes;
     if (p.prec == HPXFFT_PREC_BF16X3) {
-        // tensor-core steps: 8192 elements per CTA, 8192 / L columns
+        // tensor-core steps: nv length-16 vectors per CTA, 16 nv / L columns;
+        // 256 (four CTAs per SM) measured faster than 512 on 16384^2 (1.91 vs
+        // 2.18 ms); HPXFFT_TC_VECTORS=256|512 overrides (tuning, tests)
+        int nv = 256;
+        const char *env = std::getenv("HPXFFT_TC_VECTORS");
+        if (env && !strcmp(env, "512")) nv = 512;
         for (int step = 0; step < 2; ++step) {
             DimPlan &d = step == 0 ? p.colA : p.colB;
             const int L = step == 0 ? p.N2 : p.N1;
             if (!TcColStepLaunch::supports(L) || !factorize(L, 16, d.pp)) return false;
             d.C = 1;
             d.L = L;
-            d.log2W = TcColStepLaunch::log2W(L);
-            d.shape.threads = TcColStepLaunch::threads();
-            d.shape.smem = TcColStepLaunch::smem();
+            d.log2W = TcColStepLaunch::log2W(L, nv);
+            d.shape.threads = TcColStepLaunch::threads(nv);
+            d.shape.smem = TcColStepLaunch::smem(nv);
             d.shape.cluster = 1;
             const size_t strips = (p.dcy + ((size_t)1 << d.log2W) - 1) >> d.log2W;
             const size_t groups = step == 0 ? (size_t)p.N1 : (size_t)p.N2;
@@ -454,9 +462,10 @@ static ColStepArgs colstep_args(const hpxfft_plan_s &p, int step, const void *in
     return a;
 }
 
-// The column pass, in place on `data`: one cluster kernel or steps A and B.
+// The column pass on `data`: one cluster kernel (in place) or steps A and B
+// (step B writes `dst`, which may be `data`).
 template <class A>
-static cudaError_t run_columns(hpxfft_plan_s &p, void *data, int dir)
+static cudaError_t run_columns(hpxfft_plan_s &p, void *data, int dir, void *dst)
 {
     if (!p.col_two_step) return ColLaunch<A>::run(col_args(p, data), dir, p.col.shape, p.col.FL, p.stream);
     if (p.tc_cols) {
@@ -464,24 +473,28 @@ static cudaError_t run_columns(hpxfft_plan_s &p, void *data, int dir)
                                              p.colA.shape.grid, p.stream);
         if (e != cudaSuccess) return e;
         if ((e = cudaEventRecord(p.kev[p.next % hpxfft_plan_s::kSlots][3], p.stream)) != cudaSuccess) return e;
-        return TcColStepLaunch::run(colstep_args(p, 1, p.scratch, data), p.tc_dft, p.dev_error, dir,
+        return TcColStepLaunch::run(colstep_args(p, 1, p.scratch, dst), p.tc_dft, p.dev_error, dir,
                                     p.colB.shape.grid, p.stream);
     }
     cudaError_t e = ColStepLaunch<A>::run(colstep_args(p, 0, data, p.scratch), dir, p.colA.shape, p.colA.FL, p.stream);
     if (e != cudaSuccess) return e;
     if ((e = cudaEventRecord(p.kev[p.next % hpxfft_plan_s::kSlots][3], p.stream)) != cudaSuccess) return e;
-    return ColStepLaunch<A>::run(colstep_args(p, 1, p.scratch, data), dir, p.colB.shape, p.colB.FL, p.stream);
+    return ColStepLaunch<A>::run(colstep_args(p, 1, p.scratch, dst), dir, p.colB.shape, p.colB.FL, p.stream);
 }
 
+// Rows from `in` to `out`, columns on `out`; with the two-step column pass
+// the last step writes `final_out` when it is given (the host buffer of the
+// zero-copy path).
 template <class A>
-static cudaError_t run_forward(hpxfft_plan_s &p, const void *in, void *out)
+static cudaError_t run_forward(hpxfft_plan_s &p, const void *in, void *out, void *final_out = nullptr)
 {
     cudaError_t e;
     cudaEvent_t *ev = next_slot(p);
     if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
     if ((e = RowLaunch<A>::r2c(row_args(p, in, out, 0), p.row.shape, p.row.FL, p.stream)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
-    if ((e = run_columns<A>(p, out, -1)) != cudaSuccess) return e;
+    void *dst = final_out && p.col_two_step ? final_out : out;
+    if ((e = run_columns<A>(p, out, -1, dst)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[2], p.stream)) != cudaSuccess) return e;
     ++p.next;
     return cudaSuccess;
@@ -493,7 +506,7 @@ static cudaError_t run_inverse(hpxfft_plan_s &p, void *data, int adjoint)
     cudaError_t e;
     cudaEvent_t *ev = next_slot(p);
     if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
-    if ((e = run_columns<A>(p, data, +1)) != cudaSuccess) return e;
+    if ((e = run_columns<A>(p, data, +1, data)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
     if ((e = RowLaunch<A>::c2r(row_args(p, data, data, adjoint), p.row.shape, p.row.FL, p.stream)) != cudaSuccess)
         return e;
@@ -502,12 +515,12 @@ static cudaError_t run_inverse(hpxfft_plan_s &p, void *data, int adjoint)
     return cudaSuccess;
 }
 
-static cudaError_t dispatch_forward(hpxfft_plan_s &p, const void *in, void *out)
+static cudaError_t dispatch_forward(hpxfft_plan_s &p, const void *in, void *out, void *final_out = nullptr)
 {
     switch (p.prec) {
-    case HPXFFT_PREC_F64: return run_forward<ArithFF>(p, in, out);
-    case HPXFFT_PREC_F64_NATIVE: return run_forward<ArithF64>(p, in, out);
-    default: return run_forward<ArithF32>(p, in, out);
+    case HPXFFT_PREC_F64: return run_forward<ArithFF>(p, in, out, final_out);
+    case HPXFFT_PREC_F64_NATIVE: return run_forward<ArithF64>(p, in, out, final_out);
+    default: return run_forward<ArithF32>(p, in, out, final_out);
     }
 }
 
@@ -559,6 +572,7 @@ static int collect(hpxfft_plan_s &p)
             p.meas["h2d"] = 1e-3 * h;
             p.meas["d2h"] = 1e-3 * d;
             p.meas["e2e"] = 1e-3 * t;
+            p.meas["host_zero_copy"] = p.last_zero_copy ? 1.0 : 0.0;
             p.pending_copy = false;
         }
     }
@@ -819,6 +833,17 @@ static int check_device_error(hpxfft_plan p)
     return fail(HPXFFT_ERR_TIMEOUT, "tensor-core MMA completion wait timed out");
 }
 
+// Device address of a page-locked (pinned or registered) host buffer, else null.
+static void *mapped_host(void *h)
+{
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 int hpxfft_execute_r2c_host(hpxfft_plan p, void *h)
 {
     if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
@@ -829,14 +854,25 @@ int hpxfft_execute_r2c_host(hpxfft_plan p, void *h)
     cudaError_t e;
     if ((rc = collect(*p)) != HPXFFT_OK) return rc;
     if ((e = cudaEventRecord(p->ev_copy[0], p->stream)) != cudaSuccess) return cuda_fail(e, "event");
-    if ((e = cudaMemcpyAsync(p->dbuf, h, bytes, cudaMemcpyHostToDevice, p->stream)) != cudaSuccess)
-        return cuda_fail(e, "host to device copy");
-    if ((e = dispatch_forward(*p, p->dbuf, p->dbuf)) != cudaSuccess) return cuda_fail(e, "forward launch");
-    if ((e = cudaMemcpyAsync(h, p->dbuf, bytes, cudaMemcpyDeviceToHost, p->stream)) != cudaSuccess)
-        return cuda_fail(e, "device to host copy");
+    void *hd = ((uintptr_t)h & 15) ? nullptr : mapped_host(h);
+    if (hd) {
+        // page-locked host memory: the row pass reads it and the last column
+        // step writes it over the host link, no staging copies
+        if ((e = dispatch_forward(*p, hd, p->dbuf, hd)) != cudaSuccess) return cuda_fail(e, "forward launch");
+        if (!p->col_two_step &&
+            (e = cudaMemcpyAsync(h, p->dbuf, bytes, cudaMemcpyDeviceToHost, p->stream)) != cudaSuccess)
+            return cuda_fail(e, "device to host copy");
+    } else {
+        if ((e = cudaMemcpyAsync(p->dbuf, h, bytes, cudaMemcpyHostToDevice, p->stream)) != cudaSuccess)
+            return cuda_fail(e, "host to device copy");
+        if ((e = dispatch_forward(*p, p->dbuf, p->dbuf)) != cudaSuccess) return cuda_fail(e, "forward launch");
+        if ((e = cudaMemcpyAsync(h, p->dbuf, bytes, cudaMemcpyDeviceToHost, p->stream)) != cudaSuccess)
+            return cuda_fail(e, "device to host copy");
+    }
     if ((e = cudaEventRecord(p->ev_copy[1], p->stream)) != cudaSuccess) return cuda_fail(e, "event");
     if ((e = cudaEventSynchronize(p->ev_copy[1])) != cudaSuccess) return cuda_fail(e, "transform");
     p->pending_copy = true;
+    p->last_zero_copy = hd != nullptr;
     if ((rc = collect(*p)) != HPXFFT_OK) return rc;
     return check_device_error(p);
 }

@@ -3,7 +3,7 @@
 // Same contract as colstep_kernel (one step of the four-step column FFT,
 // nx = N1 * N2), for DFT lengths L = 16 * L2, L2 in {2, 4, 8, 16}.  The first
 // Stockham pass (radix 16, no twiddles) of every length-L transform runs on
-// the tensor cores: a CTA holds 512 length-16 vectors x (vector (j, w) =
+// the tensor cores: a CTA holds NV (512 or 256) length-16 vectors x (vector (j, w) =
 // elements j + (L/16) t, t = 0..15, of column w), and the 16-point complex DFT
 // of all of them is one real matrix product
 //     D[v][n] = sum_k A[v][k] B[k][n],   A[v] = (Re x_0..15, Im x_0..15),
@@ -11,7 +11,7 @@
 //                            S[t][q] = -+sin(2 pi q t / 16) (forward / inverse),
 // so D[v] = (Re X_0..15, Im X_0..15).  A and B are each split into three BF16
 // terms (x = x0 + x1 + x2 exactly to 24 bits) and the six products with
-// i + j <= 2 accumulate in FP32 in tensor memory: 4 blocks of 128 vectors,
+// i + j <= 2 accumulate in FP32 in tensor memory: NV / 128 blocks of 128 vectors,
 // tcgen05.mma M = 128, N = 32, K = 6 x 32.  The remaining passes, the
 // four-step twiddle and the stores run on the CUDA cores in FP32.
 //
@@ -27,16 +27,16 @@
 
 namespace hpxfft_gpu {
 
-constexpr int kTcVectors = 512;                             // length-16 vectors per CTA
-constexpr int kTcThreads = 512;                             // one vector per thread
-constexpr int kTcBlocks = kTcVectors / 128;                 // MMA row blocks
+// NV = length-16 vectors per CTA (512: 2 CTAs per SM, 256: 4 CTAs per SM),
+// one vector per thread, NV / 128 MMA row blocks.
 constexpr int kTcOperandBytes = 128 * 32 * 2;               // one 128 x 32 BF16 operand
-constexpr int kTcABytes = kTcBlocks * 3 * kTcOperandBytes;  // data splits, 96 KB
 constexpr int kTcBSplitBytes = 32 * 32 * 2;                 // one 32 x 32 BF16 DFT matrix
 constexpr int kTcBBytes = 3 * kTcBSplitBytes;               // its three splits
-constexpr int kTcTmemCols = kTcBlocks * 32;                 // FP32 accumulators, 32 columns per block
-constexpr size_t kTcSmem = kTcABytes + kTcBBytes + 128;     // + alignment slack
-static_assert((size_t)padded_elems(kTcVectors * 16) * 8 <= (size_t)kTcABytes, "FP32 tile must fit the A region");
+__host__ __device__ constexpr int tc_a_bytes(int NV) { return NV / 128 * 3 * kTcOperandBytes; }
+__host__ __device__ constexpr size_t tc_smem(int NV) { return (size_t)tc_a_bytes(NV) + kTcBBytes + 128; }
+__host__ __device__ constexpr int tc_tmem_cols(int NV) { return NV / 128 * 32; }  // FP32 accumulators
+static_assert((size_t)padded_elems(256 * 16) * 8 <= (size_t)tc_a_bytes(256), "FP32 tile must fit the A region");
+static_assert((size_t)padded_elems(512 * 16) * 8 <= (size_t)tc_a_bytes(512), "FP32 tile must fit the A region");
 
 struct TcColStepArgs {
     ColStepArgs c;
@@ -71,11 +71,15 @@ __device__ __forceinline__ void split3_bf16(const float (&v)[8], uint4 &h, uint4
     l = make_uint4(pl[0], pl[1], pl[2], pl[3]);
 }
 
-template <int DIR, int FL>
-__global__ void __launch_bounds__(kTcThreads, 2) colstep_tc_kernel(TcColStepArgs ta)
+template <int DIR, int FL, int NV>
+__global__ void __launch_bounds__(NV, 2 * 512 / NV) colstep_tc_kernel(TcColStepArgs ta)
 {
+    constexpr int kTcThreads = NV;
+    constexpr int kTcBlocks = NV / 128;
+    constexpr int kTcABytes = tc_a_bytes(NV);
+    constexpr int kTcTmemCols = tc_tmem_cols(NV);
     constexpr int LR = FL / 16;                // vectors per column
-    constexpr int W = kTcVectors / LR;         // columns per CTA
+    constexpr int W = NV / LR;                 // columns per CTA
     constexpr int log2W = ilog2c(W);
     constexpr int nel = FL * W;
     static_assert(FL % 16 == 0 && (1 << log2W) == W, "length must be 16 times a power of two");

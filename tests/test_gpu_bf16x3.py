@@ -100,3 +100,12 @@ def test_unsupported_row_counts(gpu_lib, cuda):
         with pytest.raises(gpu_lib.HpxFftError) as e:
             gpu_lib.Plan(n_row, 18, 1, "bf16x3", "estimate")
         assert e.value.status == gpu_lib._capi.HPXFFT_ERR_UNSUPPORTED_SIZE
+
+
+@pytest.mark.parametrize("nx,ny", [(1024, 96), (16384, 18), (65536, 6)])
+def test_half_occupancy_variant(gpu_lib, cuda, oracle_lib, monkeypatch, nx, ny):
+    """512 vectors per CTA (2 CTAs per SM) instead of the default 256."""
+    monkeypatch.setenv("HPXFFT_TC_VECTORS", "512")
+    x = np.random.default_rng(nx - ny).uniform(-1, 1, (nx, ny)).astype(np.float32)
+    got = forward(gpu_lib, cuda, x)
+    assert rel_l2(got, oracle_fwd(oracle_lib, x.astype(np.float64))) <= TOL, (nx, ny)
