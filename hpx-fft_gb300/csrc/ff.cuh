@@ -207,54 +207,38 @@ HPXFFT_HD ff ff_from_double(double x, int E)
     return r;
 }
 
-// (hi + lo) * 2^E rounded to double.  The pair must be renormalised
-// (|lo| <= ulp(hi)).
+// (hi + lo) * 2^E as a double.  The pair must be renormalised
+// (|lo| <= ulp(hi) / 2).  In units u = ulp(hi) / 2^29 the hi significand is
+// H = (2^23 + m_hi) 2^29 in [2^52, 2^53) and |lo| <= 2^28 u, so lo fits a
+// 32-bit integer (rounded to u: error <= 2^-53 relative) and H +- lo needs
+// at most one left shift to be normalised again.
 HPXFFT_HD double ff_to_double(ff v, int E)
 {
     const uint32_t hb = flt_bits(v.hi);
     const int fe = (int)((hb >> 23) & 0xff);
     const uint64_t sign = (uint64_t)(hb >> 31) << 63;
-    if (fe == 0xff) {  // inf / nan
-        return bits_dbl(sign | 0x7ff0000000000000ull | ((hb & 0x7fffffu) ? 0x8000000000000ull : 0ull));
-    }
-    if (fe == 0) {
+    if (fe == 0 || fe == 0xff) {
+        if (fe == 0xff)  // inf / nan
+            return bits_dbl(sign | 0x7ff0000000000000ull | ((hb & 0x7fffffu) ? 0x8000000000000ull : 0ull));
         // zero or float subnormal: tiny relative to the block; value from hi only
         if ((hb & 0x7fffffu) == 0) return bits_dbl(sign);
-        // subnormal float: exact conversion via scaling of the integer mantissa
         const double m = (double)(hb & 0x7fffffu);
         double r = m * bits_dbl((uint64_t)(1023 - 149 + E > 0 ? 1023 - 149 + E : 1) << 52);
         return (hb >> 31) ? -r : r;
     }
-    uint64_t H = (uint64_t)((hb & 0x7fffffu) | 0x800000u) << 29;  // units 2^(fe-127-52)
     const uint32_t lb = flt_bits(v.lo);
     const int le = (int)((lb >> 23) & 0xff);
-    if (le != 0 && le != 0xff) {
-        const uint64_t Lm = (uint64_t)((lb & 0x7fffffu) | 0x800000u);
-        const int sh = le - fe + 29;  // lo units 2^(le-127-23) in H units
-        uint64_t L = 0;
-        if (sh >= 0)
-            L = sh < 40 ? (Lm << sh) : 0;  // |lo| <= ulp(hi) gives sh <= 6
-        else if (sh > -40)
-            L = Lm >> (-sh);
-        if ((hb ^ lb) >> 31)
-            H -= L;
-        else
-            H += L;
-    }
+    const uint32_t ml = (lb & 0x7fffffu) | 0x800000u;
+    const int sh = le - fe + 29;  // lo = ml 2^sh u, sh <= 5
+    uint32_t L = 0;
+    if (le != 0 && le != 0xff) L = sh >= 0 ? ml << sh : (sh > -25 ? (ml + (1u << (-sh - 1))) >> -sh : 0u);
+    uint64_t H = (uint64_t)((hb & 0x7fffffu) | 0x800000u) << 29;
+    H = ((hb ^ lb) >> 31) ? H - L : H + L;
     int de = fe - 127 + 1023 + E;
-    if (H >= (1ull << 53)) {
-        H = (H >> 1) + (H & 1ull);
-        ++de;
-        if (H >= (1ull << 53)) {
-            H >>= 1;
-            ++de;
-        }
-    }
-    while (H && H < (1ull << 52)) {
+    if (H < (1ull << 52)) {  // hi a power of two, lo of the other sign
         H <<= 1;
         --de;
     }
-    if (H == 0) return bits_dbl(sign);
     if (de <= 0) return bits_dbl(sign);  // below the double normal range
     if (de >= 2047) return bits_dbl(sign | 0x7ff0000000000000ull);
     return bits_dbl(sign | ((uint64_t)de << 52) | (H & 0xfffffffffffffull));

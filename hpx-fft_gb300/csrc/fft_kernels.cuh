@@ -107,6 +107,26 @@ __device__ __forceinline__ void store_c(typename A::S *p, cpx<typename A::T> v, 
 
 __device__ __forceinline__ int scale_exp(int emax) { return (emax == 0 || emax == 0x7ff) ? 0 : emax - 1023; }
 
+// Float-float intermediates between kernels of one transform travel as raw
+// renormalised (hi, lo) pairs (16 bytes per complex, like a double2) in units
+// of 2^E, with E stored per producing block; no double conversion on either
+// side.  Blocks whose inputs are all zero carry kExpNone, which never wins a
+// maximum.
+constexpr int kExpNone = -(1 << 20);
+__device__ __forceinline__ int block_exp(int emax) { return emax == 0 ? kExpNone : scale_exp(emax); }
+
+template <class A>
+__device__ __forceinline__ void store_pair(typename A::S *p, cpx<typename A::T> v)
+{
+    if constexpr (A::kScaled) {
+        const ff re = renorm(v.re), im = renorm(v.im);
+        __stcs(reinterpret_cast<float4 *>(p), make_float4(re.hi, re.lo, im.hi, im.lo));
+    }
+}
+
+// 2^d as a float for d <= 0, flushed below the normal range
+__device__ __forceinline__ float pow2_le0(int d) { return d >= -126 ? __int_as_float((127 + d) << 23) : 0.0f; }
+
 // twiddle W_Ltab^e (table holds the forward sign); DIR > 0 conjugates
 template <int DIR, class T>
 __device__ __forceinline__ cpx<T> twid(const cpx<T> *__restrict__ tw, int e)
@@ -209,14 +229,14 @@ __device__ __forceinline__ void fixed_pass(cpx<T> *s, const cpx<T> *__restrict__
         const int task = threadIdx.x + t * NT;
         if (active && (NTASK % NT == 0 || task < NTASK)) {
             const int w = task % W, jj = task / W;
-            if constexpr (RAW) {
+            if (RAW && sEc) {
                 // first pass of the float-float path: the slots still hold the
                 // raw doubles; convert with the transform's scale exponent
                 const int E = scale_exp(sEc[w]);
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     const double2 d = reinterpret_cast<const double2 *>(s)[pidx((jj + r * LR) * W + w)];
-                    v[t][r] = cpx<T>{ff_from_double(d.x, E), ff_from_double(d.y, E)};
+                    if constexpr (RAW) v[t][r] = cpx<T>{ff_from_double(d.x, E), ff_from_double(d.y, E)};
                 }
             } else {
 #pragma unroll
@@ -353,6 +373,8 @@ struct RowArgs {
     const void *tw;           // W_{2M}^e, e in [0, 2M)
     int Ltab;                 // 2M
     const void *ptab;         // per-pass twiddles of the compile-time chain
+    int pairs_out;            // float-float r2c: store (hi, lo) pairs and one exponent per row
+    int *exp_out;             // [batch][nrows] when pairs_out
 };
 
 struct ColArgs {
@@ -485,6 +507,12 @@ __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bi
             const cpx<T> e = chalf(za + zb), o = chalf(za - zb);
             const cpx<T> tk = cmul(tw[k], o);
             S *orow = out + row * a.out_stride;
+            if (A::kScaled && a.pairs_out) {
+                store_pair<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk));
+                if (M - k != k) store_pair<A>(orow + 2 * (long long)(M - k), cconj(e + mul_i<+1>(tk)));
+                if (k == 0) a.exp_out[(long long)bidx * a.nrows + row] = block_exp(sEc[w]);
+                continue;
+            }
             store_c<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk), E);
             if (M - k != k) store_c<A>(orow + 2 * (long long)(M - k), cconj(e + mul_i<+1>(tk)), E);
         }
@@ -526,8 +554,16 @@ __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bi
             const cpx<T> tk = cmul(tw[k], o);
             S *orow = out + row0 * a.out_stride;
             if (row0 < a.nrows) {
-                store_c<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk), E);
-                if (k == 0) store_c<A>(orow + 2 * (long long)M, cconj(e + mul_i<+1>(tk)), E);
+                if (A::kScaled && a.pairs_out) {
+                    store_pair<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk));
+                    if (k == 0) {
+                        store_pair<A>(orow + 2 * (long long)M, cconj(e + mul_i<+1>(tk)));
+                        a.exp_out[(long long)bidx * a.nrows + row0] = block_exp(sEc[0]);
+                    }
+                } else {
+                    store_c<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk), E);
+                    if (k == 0) store_c<A>(orow + 2 * (long long)M, cconj(e + mul_i<+1>(tk)), E);
+                }
             }
         }
         cl.sync();
@@ -747,6 +783,8 @@ __global__ void HPXFFT_BOUNDS(A, FL) col_kernel(ColArgs a)
 // array of the same layout, B reads the scratch and writes the data, so the
 // column pass costs two HBM round trips instead of one but streams wide
 // segments with full occupancy.
+constexpr int kColStepMaxPairL = 256;  // longest step of the pair format (compiled shapes)
+
 struct ColStepArgs {
     const void *in;
     void *out;
@@ -763,6 +801,15 @@ struct ColStepArgs {
     const void *tw;           // W_nx table (post twiddle) and runtime-plan twiddles
     int Ltab;                 // nx
     const void *ptab;
+    // float-float pair format (compile-time chains only): input row r carries
+    // exponent exp_in[(r % exp_rmod) * exp_rmul + (col0 >> exp_cshift)]
+    // (per-row exponents of the row kernel, or per-block ones of step A);
+    // pairs_out stores pairs and exp_out[blockIdx.x + gridDim.x * batch]
+    int pairs_in, pairs_out;
+    const int *exp_in;
+    int exp_rmod, exp_rmul, exp_cshift;
+    long long exp_in_bstride;
+    int *exp_out;
 };
 
 template <class A, int DIR, int FL, int FW>
@@ -791,7 +838,37 @@ __global__ void HPXFFT_BOUNDS(A, FL) colstep_kernel(ColStepArgs a)
         if (col < a.ncols) v = ld_stream(in + (in_row0 + (long long)a.in_step * m) * a.row_stride + 2 * (long long)col);
         return v;
     };
-    if constexpr (A::kScaled) {
+    int Eblk = kExpNone;  // pair format: the block's common exponent
+    bool loaded = false;
+    if constexpr (A::kScaled && kFixed) {
+      if (a.pairs_in) {
+        // exponents of the L input rows, their maximum, exact power-of-two
+        // factors that bring every row to it
+        __shared__ int sEm, sExp[kColStepMaxPairL];
+        __shared__ float sFac[kColStepMaxPairL];
+        if (tid == 0) sEm = kExpNone;
+        __syncthreads();
+        const int *ein = a.exp_in + (long long)blockIdx.y * a.exp_in_bstride;
+        for (int m = tid; m < L; m += nth) {
+            const int r = (int)(in_row0 + (long long)a.in_step * m);
+            const int e = ein[(r % a.exp_rmod) * a.exp_rmul + (col0 >> a.exp_cshift)];
+            sExp[m] = e;
+            atomicMax(&sEm, e);
+        }
+        __syncthreads();
+        Eblk = sEm;
+        for (int m = tid; m < L; m += nth) sFac[m] = Eblk == kExpNone ? 1.0f : pow2_le0(sExp[m] - Eblk);
+        __syncthreads();
+        batched_loop<EPT, double2>(nel, nth, ld, [&](int t, double2 v) {
+            const float4 q = *reinterpret_cast<const float4 *>(&v);
+            const float f = sFac[t >> log2W];
+            s[pidx(t)] = cpx<T>{ff{q.x * f, q.y * f}, ff{q.z * f, q.w * f}};
+        });
+        loaded = true;
+      }
+    }
+    if (loaded) {
+    } else if constexpr (A::kScaled) {
         if (tid < 64) sE[tid] = 0;
         __syncthreads();
         int emax = 0;
@@ -812,19 +889,26 @@ __global__ void HPXFFT_BOUNDS(A, FL) colstep_kernel(ColStepArgs a)
     }
     __syncthreads();
 
+    const bool pairs_in = A::kScaled && kFixed && a.pairs_in;
     if constexpr (kFixed)
         FixedPasses<T, FL, (1 << FW), fixed_threads(FL, FW, EPT), DIR, EPT, 1, 0, A::kScaled, false>::run(
-            s, ptab, sEc, tw, 0);
+            s, ptab, pairs_in ? nullptr : sEc, tw, 0);
     else
         local_fft<T, DIR>(s, L, log2W, a.pp, tw, a.Ltab);
 
+    const bool pairs_out = pairs_in && a.pairs_out;
+    if (pairs_out && tid == 0) a.exp_out[blockIdx.x + (long long)gridDim.x * blockIdx.y] = Eblk;
     for (int t = t0; t < nel; t += nth) {
         const int w = t & wmask, k = t >> log2W, col = col0 + w;
         if (col >= a.ncols) continue;
-        const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
+        const int E = A::kScaled ? (pairs_in ? (Eblk == kExpNone ? 0 : Eblk) : scale_exp(sEc[w])) : 0;
         cpx<T> v = s[pidx(t)];
         if (a.post && g) v = cmul(v, twid<DIR>(tw, g * k));
-        store_c<A>(out + (out_row0 + (long long)a.out_step * k) * a.row_stride + 2 * (long long)col, v, E);
+        S *o = out + (out_row0 + (long long)a.out_step * k) * a.row_stride + 2 * (long long)col;
+        if (pairs_out)
+            store_pair<A>(o, v);
+        else
+            store_c<A>(o, v, E);
     }
 }
 

@@ -62,6 +62,11 @@ struct hpxfft_plan_s {
     int N1 = 0, N2 = 0;
     hpxfft_gpu::DimPlan colA, colB;
     void *scratch = nullptr;
+    // float-float forward two-step pass: rows -> step A -> step B exchange
+    // raw (hi, lo) pairs with per-row / per-block exponents instead of doubles
+    bool ff_pairs = false;
+    int *exp_rows = nullptr;   // [batch][nx]
+    int *exp_step_a = nullptr; // [batch][step A blocks]
     // split-BF16 precision: both column steps on the tensor cores
     bool tc_cols = false;
     void *tc_dft = nullptr;     // BF16 DFT-16 matrix splits
@@ -192,6 +197,16 @@ static bool plan_cols(hpxfft_plan_s &p)
     return false;
 }
 
+static bool has_fixed_step(int prec, const DimPlan &d)
+{
+    switch (prec) {
+    case HPXFFT_PREC_F64: return ColStepLaunch<ArithFF>::has_fixed(d.L, d.log2W);
+    case HPXFFT_PREC_F32: return ColStepLaunch<ArithF32>::has_fixed(d.L, d.log2W);
+    case HPXFFT_PREC_BF16X3: return TcColStepLaunch::supports(d.L);  // FP32 chain after the tensor-core pass
+    default: return false;
+    }
+}
+
 // Shapes of the two-kernel column pass for power-of-two nx >= 1024:
 // N2 = 2^floor(log2(nx)/2) (step A length), N1 = nx / N2 (step B length),
 // strips of up to 64 columns.
@@ -235,6 +250,13 @@ static bool plan_colsteps(hpxfft_plan_s &p)
         int log2W = wcap;
         while (log2W > 0 && (L << log2W) > maxel) --log2W;
         if ((L << log2W) > maxel) return false;
+        // narrow arrays keep the compiled strip width (idle columns are
+        // masked) rather than fall back to the runtime-plan kernel
+        int full = 6;
+        while (full > 0 && (L << full) > maxel) --full;
+        d.L = L;
+        d.log2W = full;
+        if (full > log2W && has_fixed_step(p.prec, d)) log2W = full;
         PassPlan pp;
         if (!factorize(L, 16, pp)) return false;
         d.C = 1;
@@ -270,16 +292,6 @@ static cudaError_t prepare_once()
     if (e == cudaSuccess) e = ColStepLaunch<A>::prepare();
     if (e == cudaSuccess) done[dev] = true;
     return e;
-}
-
-static bool has_fixed_step(int prec, const DimPlan &d)
-{
-    switch (prec) {
-    case HPXFFT_PREC_F64: return ColStepLaunch<ArithFF>::has_fixed(d.L, d.log2W);
-    case HPXFFT_PREC_F32: return ColStepLaunch<ArithF32>::has_fixed(d.L, d.log2W);
-    case HPXFFT_PREC_BF16X3: return TcColStepLaunch::supports(d.L);  // FP32 chain after the tensor-core pass
-    default: return false;
-    }
 }
 
 static bool has_fixed(int prec, bool rows, const DimPlan &d)
@@ -399,6 +411,8 @@ static RowArgs row_args(const hpxfft_plan_s &p, const void *in, void *out, int a
     a.tw = p.tw_row;
     a.Ltab = (int)(2 * p.M);
     a.ptab = p.row.ptab;
+    a.pairs_out = 0;
+    a.exp_out = nullptr;
     return a;
 }
 
@@ -432,7 +446,7 @@ static cudaEvent_t *next_slot(hpxfft_plan_s &p)
     return p.kev[p.next % hpxfft_plan_s::kSlots];
 }
 
-static ColStepArgs colstep_args(const hpxfft_plan_s &p, int step, const void *in, void *out)
+static ColStepArgs colstep_args(const hpxfft_plan_s &p, int step, const void *in, void *out, bool pairs = false)
 {
     const DimPlan &d = step == 0 ? p.colA : p.colB;
     ColStepArgs a{};
@@ -459,6 +473,23 @@ static ColStepArgs colstep_args(const hpxfft_plan_s &p, int step, const void *in
     a.tw = p.tw_col;
     a.Ltab = (int)p.nx;
     a.ptab = d.ptab;
+    if (pairs && step == 0) {  // per-row exponents of the row kernel
+        a.pairs_in = a.pairs_out = 1;
+        a.exp_in = p.exp_rows;
+        a.exp_rmod = 1 << 30;
+        a.exp_rmul = 1;
+        a.exp_cshift = 30;
+        a.exp_in_bstride = (long long)p.nx;
+        a.exp_out = p.exp_step_a;
+    } else if (pairs) {  // scratch row N1 g + m came from step A block (m, strip)
+        const int strips_a = (int)((p.dcy + ((size_t)1 << p.colA.log2W) - 1) >> p.colA.log2W);
+        a.pairs_in = 1;
+        a.exp_in = p.exp_step_a;
+        a.exp_rmod = p.N1;
+        a.exp_rmul = strips_a;
+        a.exp_cshift = p.colA.log2W;
+        a.exp_in_bstride = (long long)p.colA.shape.grid.x;
+    }
     return a;
 }
 
@@ -476,10 +507,12 @@ static cudaError_t run_columns(hpxfft_plan_s &p, void *data, int dir, void *dst)
         return TcColStepLaunch::run(colstep_args(p, 1, p.scratch, dst), p.tc_dft, p.dev_error, dir,
                                     p.colB.shape.grid, p.stream);
     }
-    cudaError_t e = ColStepLaunch<A>::run(colstep_args(p, 0, data, p.scratch), dir, p.colA.shape, p.colA.FL, p.stream);
+    const bool pairs = p.ff_pairs && dir < 0;
+    cudaError_t e =
+        ColStepLaunch<A>::run(colstep_args(p, 0, data, p.scratch, pairs), dir, p.colA.shape, p.colA.FL, p.stream);
     if (e != cudaSuccess) return e;
     if ((e = cudaEventRecord(p.kev[p.next % hpxfft_plan_s::kSlots][3], p.stream)) != cudaSuccess) return e;
-    return ColStepLaunch<A>::run(colstep_args(p, 1, p.scratch, dst), dir, p.colB.shape, p.colB.FL, p.stream);
+    return ColStepLaunch<A>::run(colstep_args(p, 1, p.scratch, dst, pairs), dir, p.colB.shape, p.colB.FL, p.stream);
 }
 
 // Rows from `in` to `out`, columns on `out`; with the two-step column pass
@@ -491,7 +524,12 @@ static cudaError_t run_forward(hpxfft_plan_s &p, const void *in, void *out, void
     cudaError_t e;
     cudaEvent_t *ev = next_slot(p);
     if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
-    if ((e = RowLaunch<A>::r2c(row_args(p, in, out, 0), p.row.shape, p.row.FL, p.stream)) != cudaSuccess) return e;
+    RowArgs ra = row_args(p, in, out, 0);
+    if (p.ff_pairs) {
+        ra.pairs_out = 1;
+        ra.exp_out = p.exp_rows;
+    }
+    if ((e = RowLaunch<A>::r2c(ra, p.row.shape, p.row.FL, p.stream)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
     void *dst = final_out && p.col_two_step ? final_out : out;
     if ((e = run_columns<A>(p, out, -1, dst)) != cudaSuccess) return e;
@@ -726,6 +764,19 @@ int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
             }
         }
     }
+    // float-float pair exchange between the forward kernels (compiled step
+    // shapes only); HPXFFT_FF_PAIRS=0 keeps doubles in between (tests, tuning)
+    const char *pairs_env = std::getenv("HPXFFT_FF_PAIRS");
+    if (rc == HPXFFT_OK && precision == HPXFFT_PREC_F64 && p->col_two_step && p->colA.FL && p->colB.FL &&
+        p->colA.L <= kColStepMaxPairL && p->colB.L <= kColStepMaxPairL && !(pairs_env && !strcmp(pairs_env, "0"))) {
+        if (cudaMalloc(&p->exp_rows, sizeof(int) * p->nx * p->batch) != cudaSuccess ||
+            cudaMalloc(&p->exp_step_a, sizeof(int) * p->colA.shape.grid.x * p->batch) != cudaSuccess) {
+            cudaGetLastError();
+            rc = fail(HPXFFT_ERR_ALLOC, "exponent arrays");
+        } else {
+            p->ff_pairs = true;
+        }
+    }
     if (rc != HPXFFT_OK) {
         std::string msg = g_last_error;
         hpxfft_plan_destroy(p);
@@ -763,6 +814,8 @@ int hpxfft_plan_destroy(hpxfft_plan p)
     cudaFree(p->dbuf);
     cudaFree(p->tc_dft);
     cudaFree(p->dev_error);
+    cudaFree(p->exp_rows);
+    cudaFree(p->exp_step_a);
     for (auto &slot : p->kev)
         for (auto &ev : slot)
             if (ev) cudaEventDestroy(ev);
@@ -950,7 +1003,8 @@ int hpxfft_write_plan(hpxfft_plan p, const char *path)
     if (!f) return fail(HPXFFT_ERR_IO, std::string("Failed to open file: ") + path);
     fprintf(f, "GPU r2c 1D plan:\n%s\n", describe(*p, p->row, "r2c", p->ny).c_str());
     if (p->col_two_step) {
-        fprintf(f, "GPU c2c 1D plan (four-step, %d x %d):\n%s\n%s\n\n", p->N1, p->N2,
+        fprintf(f, "GPU c2c 1D plan (four-step, %d x %d%s):\n%s\n%s\n\n", p->N1, p->N2,
+                p->ff_pairs ? ", float-float pairs between kernels" : "",
                 describe(*p, p->colA, "c2c-stepA", (size_t)p->N2).c_str(),
                 describe(*p, p->colB, "c2c-stepB", (size_t)p->N1).c_str());
     } else {

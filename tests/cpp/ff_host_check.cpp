@@ -33,4 +33,9 @@ void ff_binop(const double *a, const double *b, double *y, size_t n, int op)
     }
 }
 int dbl_exp(double x) { return hpxfft_gpu::dbl_biased_exp(x); }
+// renormalised pair (hi, lo) -> double with scale 2^E
+void ff_pair_to_double(const float *hi, const float *lo, double *y, size_t n, int E)
+{
+    for (size_t i = 0; i < n; ++i) y[i] = hpxfft_gpu::ff_to_double(hpxfft_gpu::renorm(ff{hi[i], lo[i]}), E);
+}
 }

@@ -93,6 +93,25 @@ def test_float_float_special_values(ffhost):
     assert y[6] == 1.5 and y[7] == -3.25
 
 
+def test_float_float_pair_to_double(ffhost):
+    """Pairs with |lo| <= ulp(hi)/2, including powers of two with a negative
+    lo (the one-bit renormalisation) and zero lo, against the exact sum."""
+    rng = np.random.default_rng(13)
+    n = 40000
+    hi = rng.standard_normal(n).astype(np.float32)
+    hi[:2000] = np.float32(2.0) ** rng.integers(-20, 20, 2000).astype(np.float32)
+    ulp = np.spacing(np.abs(hi)).astype(np.float64)
+    lo = (rng.uniform(-0.5, 0.5, n) * ulp).astype(np.float32)
+    lo[:1000] = -np.abs(lo[:1000])
+    lo[-1000:] = 0
+    y = np.zeros(n)
+    fp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    for E in (-60, 0, 37):
+        ffhost.ff_pair_to_double(fp(hi), fp(lo), _dp(y), n, E)
+        exact = (hi.astype(np.float64) + lo.astype(np.float64)) * 2.0**E
+        assert np.max(np.abs(y - exact) / np.abs(exact)) <= 2.0**-52
+
+
 def test_float_float_arithmetic(ffhost):
     rng = np.random.default_rng(12)
     a, b = rng.standard_normal(20000), rng.standard_normal(20000)
