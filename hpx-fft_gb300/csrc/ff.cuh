@@ -169,7 +169,7 @@ HPXFFT_HD int dbl_biased_exp(double x) { return (int)((dbl_bits(x) >> 52) & 0x7f
 // lo the next 29 bits rounded to 24.  Values whose scaled magnitude falls
 // below the float normal range are flushed to zero: with E the exponent of
 // the transform's largest input they are < 2^-126 of it.
-HPXFFT_HD ff ff_from_double(double x, int E)
+HPXFFT_HD ff ff_from_double_int(double x, int E)
 {
     const uint64_t b = dbl_bits(x);
     const uint32_t hi32 = (uint32_t)(b >> 32);
@@ -207,12 +207,32 @@ HPXFFT_HD ff ff_from_double(double x, int E)
     return r;
 }
 
-// (hi + lo) * 2^E as a double.  The pair must be renormalised
+// The same for the common case (scaled exponent well inside the float range,
+// not inf / nan / zero / subnormal): hi from the top bits by a funnel shift,
+// lo = (next 29 bits, converted and rounded to 24) * 2^(fe - 179).
+HPXFFT_HD ff ff_from_double(double x, int E)
+{
+    const uint64_t b = dbl_bits(x);
+    const uint32_t hi32 = (uint32_t)(b >> 32);
+    const uint32_t lo32 = (uint32_t)b;
+    const int e = (int)((hi32 >> 20) & 0x7ff);
+    const int fe = e - 1023 + 127 - E;
+    if (e == 0 || e == 0x7ff || fe < 60 || fe > 254) return ff_from_double_int(x, E);
+    const uint32_t sign = hi32 & 0x80000000u;
+    const uint32_t top23 = (uint32_t)(b >> 29) & 0x7fffffu;
+    ff r;
+    r.hi = bits_flt(sign | ((uint32_t)fe << 23) | top23);
+    const float mag = (float)(lo32 & 0x1fffffffu) * bits_flt((uint32_t)(fe - 52) << 23);
+    r.lo = bits_flt(flt_bits(mag) ^ sign);
+    return r;
+}
+
+// (hi + lo) * 2^E as a double, integer operations only.  The pair must be renormalised
 // (|lo| <= ulp(hi) / 2).  In units u = ulp(hi) / 2^29 the hi significand is
 // H = (2^23 + m_hi) 2^29 in [2^52, 2^53) and |lo| <= 2^28 u, so lo fits a
 // 32-bit integer (rounded to u: error <= 2^-53 relative) and H +- lo needs
 // at most one left shift to be normalised again.
-HPXFFT_HD double ff_to_double(ff v, int E)
+HPXFFT_HD double ff_to_double_int(ff v, int E)
 {
     const uint32_t hb = flt_bits(v.hi);
     const int fe = (int)((hb >> 23) & 0xff);
@@ -242,6 +262,37 @@ HPXFFT_HD double ff_to_double(ff v, int E)
     if (de <= 0) return bits_dbl(sign);  // below the double normal range
     if (de >= 2047) return bits_dbl(sign | 0x7ff0000000000000ull);
     return bits_dbl(sign | ((uint64_t)de << 52) | (H & 0xfffffffffffffull));
+}
+
+HPXFFT_HD int f2i_rn(float x)
+{
+#ifdef __CUDA_ARCH__
+    return __float2int_rn(x);
+#else
+    return (int)std::lrintf(x);
+#endif
+}
+
+// The same, with the float unit doing the alignment: lo, with the sign of hi
+// folded in, times 2^(179 - fe) is |lo| in units u = 2^(fe - 179) (exact:
+// a power-of-two scale), rounded to an integer (|L| <= 2^28); then one 64-bit
+// add onto the hi significand.  Exponents near the ends of the float or
+// double range take the integer path.
+HPXFFT_HD double ff_to_double(ff v, int E)
+{
+    const uint32_t hb = flt_bits(v.hi);
+    const int fe = (int)((hb >> 23) & 0xff);
+    const int de = fe - 127 + 1023 + E;
+    if (fe < 60 || fe == 0xff || de < 2 || de > 2045) return ff_to_double_int(v, E);
+    const float lo_rel = bits_flt(flt_bits(v.lo) ^ (hb & 0x80000000u));
+    const int L = f2i_rn(lo_rel * bits_flt((uint32_t)(306 - fe) << 23));
+    const uint64_t H = ((uint64_t)((hb & 0x7fffffu) | 0x800000u) << 29) + (uint64_t)(int64_t)L;
+    uint64_t bits;
+    if (H >> 52)
+        bits = ((uint64_t)de << 52) | (H & 0xfffffffffffffull);
+    else  // hi a power of two, lo of the other sign: one bit lower
+        bits = ((uint64_t)(de - 1) << 52) | ((H << 1) & 0xfffffffffffffull);
+    return bits_dbl(((uint64_t)(hb >> 31) << 63) | bits);
 }
 
 }  // namespace hpxfft_gpu

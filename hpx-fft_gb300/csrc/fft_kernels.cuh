@@ -375,6 +375,7 @@ struct RowArgs {
     const void *ptab;         // per-pass twiddles of the compile-time chain
     int pairs_out;            // float-float r2c: store (hi, lo) pairs and one exponent per row
     int *exp_out;             // [batch][nrows] when pairs_out
+    int prefetch;             // persistent r2c: prefetch the next row group into L2 (device input only)
 };
 
 struct ColArgs {
@@ -570,10 +571,52 @@ __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bi
     }
 }
 
+// Bring [p, p + bytes) into L2 with bulk prefetches of whole 16-byte units
+// (the ragged ends are left out), spread over the CTA's threads.
+__device__ __forceinline__ void prefetch_l2(const void *p, long long bytes)
+{
+    const uintptr_t b = ((uintptr_t)p + 15) & ~(uintptr_t)15;
+    const uintptr_t e = ((uintptr_t)p + (uintptr_t)bytes) & ~(uintptr_t)15;
+    constexpr uintptr_t kChunk = 16384;
+    for (uintptr_t c = b + threadIdx.x * kChunk; c < e; c += blockDim.x * kChunk) {
+        const unsigned sz = (unsigned)(e - c < kChunk ? e - c : kChunk);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(c), "r"(sz) : "memory");
+    }
+}
+
+// Rows whose CTA fills an SM (compile-time shapes above kFixedThreadsMax
+// threads: one 8192-pair float-float row) run persistent: a CTA walks row
+// groups blockIdx.x, blockIdx.x + gridDim.x, ... and prefetches the next
+// group's input into L2 while it transforms the current one, so its load
+// phase no longer leaves the SM idle.  Smaller shapes run two CTAs per SM,
+// which overlap each other (and the loop would cost them registers).
+template <class A>
+__host__ __device__ constexpr bool row_persistent(int C, int FL, int FW)
+{
+    return C == 1 && FL > 0 && fixed_threads(FL, FW, A::kEPTFixed) > kFixedThreadsMax;
+}
+
 template <class A, int C, int FL, int FW>
 __global__ void HPXFFT_BOUNDS(A, FL) row_r2c_kernel(RowArgs a)
 {
-    row_r2c_body<A, C, FL, FW>(a, blockIdx.x / C, blockIdx.y);
+    if constexpr (row_persistent<A>(C, FL, FW)) {
+        using S = typename A::S;
+        const int log2W = FL > 0 ? FW : a.log2W;
+        const int ngroups = (a.nrows + (1 << log2W) - 1) >> log2W;
+        for (int group = blockIdx.x; group < ngroups; group += gridDim.x) {
+            const int next = group + gridDim.x;
+            if (a.prefetch && next < ngroups) {
+                const int r0 = next << log2W, nr = min(1 << log2W, a.nrows - r0);
+                const S *src = reinterpret_cast<const S *>(a.in) + (long long)blockIdx.y * a.in_bstride +
+                               (long long)r0 * a.in_stride;
+                prefetch_l2(src, (long long)nr * a.in_stride * (long long)sizeof(S));
+            }
+            row_r2c_body<A, 1, FL, FW>(a, group, blockIdx.y);
+            __syncthreads();  // shared memory is reused by the next group
+        }
+    } else {
+        row_r2c_body<A, C, FL, FW>(a, blockIdx.x / C, blockIdx.y);
+    }
 }
 
 // ------------------------------------------------------------ row c2r kernel

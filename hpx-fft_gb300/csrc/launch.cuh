@@ -4,6 +4,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "fft_kernels.cuh"
 
 namespace hpxfft_gpu {
@@ -95,6 +97,48 @@ static cudaError_t launch_cluster(K kernel, const Args &a, const LaunchShape &s,
     return cudaLaunchKernelEx(&cfg, kernel, a);
 }
 
+// CTAs of `kernel` with shape s resident on the device at once, cached per
+// kernel, device and shape in a fixed table (no heap use: the allocation-free
+// entry point launches these kernels too); 0 if the query fails.
+struct ResidentEntry {
+    const void *kernel;
+    int dev, threads;
+    size_t smem;
+    int n;
+};
+template <class K>
+static int resident_ctas(K kernel, const LaunchShape &s)
+{
+    static std::mutex mu;
+    static ResidentEntry table[128];
+    static int used = 0;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    std::lock_guard<std::mutex> lock(mu);
+    for (int i = 0; i < used; ++i)
+        if (table[i].kernel == (const void *)kernel && table[i].dev == dev && table[i].threads == s.threads &&
+            table[i].smem == s.smem)
+            return table[i].n;
+    int per_sm = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, s.threads, s.smem) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    if (used < 128) table[used++] = ResidentEntry{(const void *)kernel, dev, s.threads, s.smem, per_sm * sms};
+    return per_sm * sms;
+}
+
+// A grid of at most one wave for a kernel that loops over its blocks' work.
+template <class K, class Args>
+static cudaError_t launch_persistent(K kernel, const Args &a, const LaunchShape &s, cudaStream_t st)
+{
+    LaunchShape p = s;
+    const int n = resident_ctas(kernel, s);
+    if (n > 0 && (int)p.grid.x > n) p.grid.x = (unsigned)n;
+    return launch_cluster(kernel, a, p, st);
+}
+
 template <class K>
 static cudaError_t set_attrs(K kernel, bool nonportable)
 {
@@ -154,8 +198,10 @@ cudaError_t RowLaunch<A>::r2c(const RowArgs &a, const LaunchShape &s, int FL, cu
 {
     if constexpr (A::kFixedChains) {
         if (FL) {
-#define HPXFFT_X(L_, W_, C_) \
-    if (FL == L_ && a.log2W == W_ && s.cluster == C_) return launch_cluster(row_r2c_kernel<A, C_, L_, W_>, a, s, st);
+#define HPXFFT_X(L_, W_, C_)                                                                            \
+    if (FL == L_ && a.log2W == W_ && s.cluster == C_)                                                   \
+        return row_persistent<A>(C_, L_, W_) ? launch_persistent(row_r2c_kernel<A, C_, L_, W_>, a, s, st) \
+                       : launch_cluster(row_r2c_kernel<A, C_, L_, W_>, a, s, st);
             if constexpr (sizeof(typename A::S) == 4) {
                 HPXFFT_ROW_FIXED_F32(HPXFFT_X)
             } else {

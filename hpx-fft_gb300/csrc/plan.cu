@@ -519,12 +519,14 @@ static cudaError_t run_columns(hpxfft_plan_s &p, void *data, int dir, void *dst)
 // the last step writes `final_out` when it is given (the host buffer of the
 // zero-copy path).
 template <class A>
-static cudaError_t run_forward(hpxfft_plan_s &p, const void *in, void *out, void *final_out = nullptr)
+static cudaError_t run_forward(hpxfft_plan_s &p, const void *in, void *out, void *final_out = nullptr,
+                               int prefetch_in = 1)
 {
     cudaError_t e;
     cudaEvent_t *ev = next_slot(p);
     if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
     RowArgs ra = row_args(p, in, out, 0);
+    ra.prefetch = prefetch_in;
     if (p.ff_pairs) {
         ra.pairs_out = 1;
         ra.exp_out = p.exp_rows;
@@ -553,12 +555,14 @@ static cudaError_t run_inverse(hpxfft_plan_s &p, void *data, int adjoint)
     return cudaSuccess;
 }
 
-static cudaError_t dispatch_forward(hpxfft_plan_s &p, const void *in, void *out, void *final_out = nullptr)
+// prefetch_in = 0 when `in` is host memory read over the host link
+static cudaError_t dispatch_forward(hpxfft_plan_s &p, const void *in, void *out, void *final_out = nullptr,
+                                   int prefetch_in = 1)
 {
     switch (p.prec) {
-    case HPXFFT_PREC_F64: return run_forward<ArithFF>(p, in, out, final_out);
-    case HPXFFT_PREC_F64_NATIVE: return run_forward<ArithF64>(p, in, out, final_out);
-    default: return run_forward<ArithF32>(p, in, out, final_out);
+    case HPXFFT_PREC_F64: return run_forward<ArithFF>(p, in, out, final_out, prefetch_in);
+    case HPXFFT_PREC_F64_NATIVE: return run_forward<ArithF64>(p, in, out, final_out, prefetch_in);
+    default: return run_forward<ArithF32>(p, in, out, final_out, prefetch_in);
     }
 }
 
@@ -911,7 +915,7 @@ int hpxfft_execute_r2c_host(hpxfft_plan p, void *h)
     if (hd) {
         // page-locked host memory: the row pass reads it and the last column
         // step writes it over the host link, no staging copies
-        if ((e = dispatch_forward(*p, hd, p->dbuf, hd)) != cudaSuccess) return cuda_fail(e, "forward launch");
+        if ((e = dispatch_forward(*p, hd, p->dbuf, hd, 0)) != cudaSuccess) return cuda_fail(e, "forward launch");
         if (!p->col_two_step &&
             (e = cudaMemcpyAsync(h, p->dbuf, bytes, cudaMemcpyDeviceToHost, p->stream)) != cudaSuccess)
             return cuda_fail(e, "device to host copy");
