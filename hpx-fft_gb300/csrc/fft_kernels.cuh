@@ -955,6 +955,167 @@ __global__ void HPXFFT_BOUNDS(A, FL) colstep_kernel(ColStepArgs a)
     }
 }
 
+// Ls of the last pass of the compile-time chain for length L, and the
+// per-pass table offset of the pass at Ls (the layout FixedPasses uses).
+__host__ __device__ constexpr int last_pass_ls(int L, int maxR)
+{
+    int Ls = 1;
+    while (Ls * fixed_radix(L, Ls, maxR) < L) Ls *= fixed_radix(L, Ls, maxR);
+    return Ls;
+}
+__host__ __device__ constexpr int pass_table_offset(int L, int maxR, int upto)
+{
+    int Ls = 1, off = 0;
+    while (Ls < upto) {
+        const int R = fixed_radix(L, Ls, maxR);
+        if (Ls > 1) off += Ls * (R - 1);
+        Ls *= R;
+    }
+    return off;
+}
+
+// The compile-time chain's passes with Ls in [Ls, END), through shared memory.
+template <class T, int L, int W, int NT, int DIR, int MAXR, int Ls, int Off, int END>
+struct FixedPassRange {
+    static __device__ __forceinline__ void run(cpx<T> *s, const cpx<T> *__restrict__ ptab)
+    {
+        if constexpr (Ls < END) {
+            constexpr int R = fixed_radix(L, Ls, MAXR);
+            fixed_pass<T, R, L, W, NT, DIR, Ls, false, false>(s, ptab + Off, nullptr, nullptr, 0);
+            FixedPassRange<T, L, W, NT, DIR, MAXR, Ls * R, Off + Ls * (R - 1), END>::run(s, ptab);
+        }
+    }
+};
+
+// A column step with the first pass fed from global memory and the last
+// pass written to it, so shared memory only carries the transposes between
+// passes (one round trip for L = 128 in FP32 instead of three).  Same
+// contract as colstep_kernel.  Written for FP32 and for float-float with
+// pair input (the block's scale comes from the producers' exponents, so no
+// data-dependent reduction has to precede the first pass); the launcher
+// uses it for FP32.
+template <class A, int DIR, int FL, int FW>
+__global__ void __launch_bounds__(fixed_threads(FL, FW, A::kEPTFixed),
+                                  fixed_threads(FL, FW, A::kEPTFixed) <= kFixedThreadsMax ? kFixedMinBlocks : 1)
+    colstep_direct_kernel(ColStepArgs a)
+{
+    using T = typename A::T;
+    using S = typename A::S;
+    constexpr int EPT = A::kEPTFixed;
+    constexpr int W = 1 << FW;
+    constexpr int NT = fixed_threads(FL, FW, EPT);
+    constexpr int R1 = fixed_radix(FL, 1, EPT), LR1 = FL / R1;
+    constexpr int LSL = last_pass_ls(FL, EPT), RL = fixed_radix(FL, LSL, EPT), LRL = FL / RL;
+    static_assert(LSL > 1, "at least two passes");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cpx<T> *s = reinterpret_cast<cpx<T> *>(smem_raw);
+    const int tid = threadIdx.x;
+    const int g = blockIdx.x / a.strips, col0 = (blockIdx.x % a.strips) * W;
+    const S *in = reinterpret_cast<const S *>(a.in) + (long long)blockIdx.y * a.in_bstride;
+    S *out = reinterpret_cast<S *>(a.out) + (long long)blockIdx.y * a.out_bstride;
+    const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
+    const cpx<T> *ptab = reinterpret_cast<const cpx<T> *>(a.ptab);
+    const long long in_row0 = (long long)g * a.in_gmul, out_row0 = (long long)g * a.out_gmul;
+
+    int Eblk = kExpNone;
+    [[maybe_unused]] float *fac = nullptr;
+    if constexpr (A::kScaled) {
+        __shared__ int sEm, sExp[kColStepMaxPairL];
+        __shared__ float sFac[kColStepMaxPairL];
+        if (tid == 0) sEm = kExpNone;
+        __syncthreads();
+        const int *ein = a.exp_in + (long long)blockIdx.y * a.exp_in_bstride;
+        for (int m = tid; m < FL; m += NT) {
+            const int r = (int)(in_row0 + (long long)a.in_step * m);
+            const int e = ein[(r % a.exp_rmod) * a.exp_rmul + (col0 >> a.exp_cshift)];
+            sExp[m] = e;
+            atomicMax(&sEm, e);
+        }
+        __syncthreads();
+        Eblk = sEm;
+        for (int m = tid; m < FL; m += NT) sFac[m] = Eblk == kExpNone ? 1.0f : pow2_le0(sExp[m] - Eblk);
+        __syncthreads();
+        fac = sFac;
+    }
+
+    // first pass: task (jj, w) takes elements jj + LR1 r of column w
+    {
+        constexpr int NTASK = LR1 * W, TPT = (NTASK + NT - 1) / NT;
+#pragma unroll
+        for (int t = 0; t < TPT; ++t) {
+            const int task = tid + t * NT;
+            if (NTASK % NT == 0 || task < NTASK) {
+                const int w = task % W, jj = task / W, col = col0 + w;
+                const bool live = col < a.ncols;
+                cpx<T> v[R1];
+                using V2 = typename std::conditional<sizeof(S) == 8, double2, float2>::type;
+                V2 raw[R1];
+#pragma unroll
+                for (int r = 0; r < R1; ++r) {
+                    raw[r] = V2{};
+                    if (live)
+                        raw[r] = ld_stream(in + (in_row0 + (long long)a.in_step * (jj + r * LR1)) * a.row_stride +
+                                           2 * (long long)col);
+                }
+#pragma unroll
+                for (int r = 0; r < R1; ++r) {
+                    if constexpr (A::kScaled) {
+                        const float4 q = *reinterpret_cast<const float4 *>(&raw[r]);
+                        const float f = fac[jj + r * LR1];
+                        v[r] = cpx<T>{ff{q.x * f, q.y * f}, ff{q.z * f, q.w * f}};
+                    } else {
+                        v[r] = cpx<T>{(T)raw[r].x, (T)raw[r].y};
+                    }
+                }
+                DFT<R1, DIR, T>::run(v);
+#pragma unroll
+                for (int r = 0; r < R1; ++r) s[pidx((jj * R1 + r) * W + w)] = cnorm(v[r]);
+            }
+        }
+    }
+    __syncthreads();
+
+    FixedPassRange<T, FL, W, NT, DIR, EPT, R1, 0, LSL>::run(s, ptab);
+
+    // last pass: outputs k = base + r LSL go straight to their rows
+    const bool pairs_out = A::kScaled && a.pairs_out;
+    if (pairs_out && tid == 0) a.exp_out[blockIdx.x + (long long)gridDim.x * blockIdx.y] = Eblk;
+    const int E = Eblk == kExpNone ? 0 : Eblk;
+    {
+        constexpr int Off = pass_table_offset(FL, EPT, LSL);
+        constexpr int NTASK = LRL * W, TPT = (NTASK + NT - 1) / NT;
+        const cpx<T> *tp = ptab + Off;
+#pragma unroll
+        for (int t = 0; t < TPT; ++t) {
+            const int task = tid + t * NT;
+            if (NTASK % NT == 0 || task < NTASK) {
+                const int w = task % W, jj = task / W, col = col0 + w;
+                const int k = jj % LSL;
+                cpx<T> v[RL];
+#pragma unroll
+                for (int r = 0; r < RL; ++r) v[r] = s[pidx((jj + r * LRL) * W + w)];
+#pragma unroll
+                for (int r = 1; r < RL; ++r) v[r] = cmul(v[r], twid<DIR>(tp, (r - 1) * LSL + k));
+                DFT<RL, DIR, T>::run(v);
+                if (col < a.ncols) {
+                    const int base = (jj - k) * RL + k;
+#pragma unroll
+                    for (int r = 0; r < RL; ++r) {
+                        const int kk = base + r * LSL;
+                        cpx<T> o = v[r];
+                        if (a.post && g) o = cmul(o, twid<DIR>(tw, g * kk));
+                        S *dst = out + (out_row0 + (long long)a.out_step * kk) * a.row_stride + 2 * (long long)col;
+                        if (pairs_out)
+                            store_pair<A>(dst, o);
+                        else
+                            store_c<A>(dst, o, E);
+                    }
+                }
+            }
+        }
+    }
+}
+
 // --------------------------------------------------------- twiddle tables
 // W_N^e = exp(-2 pi i e / N) from FP64 sincospi, rounded once to the compute
 // type (float-float keeps 48 of its 53 bits).
