@@ -307,6 +307,38 @@ struct FixedPasses {
     }
 };
 
+// Ls of the last pass of the compile-time chain for length L, and the
+// per-pass table offset of the pass at Ls (the layout FixedPasses uses).
+__host__ __device__ constexpr int last_pass_ls(int L, int maxR)
+{
+    int Ls = 1;
+    while (Ls * fixed_radix(L, Ls, maxR) < L) Ls *= fixed_radix(L, Ls, maxR);
+    return Ls;
+}
+__host__ __device__ constexpr int pass_table_offset(int L, int maxR, int upto)
+{
+    int Ls = 1, off = 0;
+    while (Ls < upto) {
+        const int R = fixed_radix(L, Ls, maxR);
+        if (Ls > 1) off += Ls * (R - 1);
+        Ls *= R;
+    }
+    return off;
+}
+
+// The compile-time chain's passes with Ls in [Ls, END), through shared memory.
+template <class T, int L, int W, int NT, int DIR, int MAXR, int Ls, int Off, int END>
+struct FixedPassRange {
+    static __device__ __forceinline__ void run(cpx<T> *s, const cpx<T> *__restrict__ ptab)
+    {
+        if constexpr (Ls < END) {
+            constexpr int R = fixed_radix(L, Ls, MAXR);
+            fixed_pass<T, R, L, W, NT, DIR, Ls, false, false>(s, ptab + Off, nullptr, nullptr, 0);
+            FixedPassRange<T, L, W, NT, DIR, MAXR, Ls * R, Off + Ls * (R - 1), END>::run(s, ptab);
+        }
+    }
+};
+
 // threads of a fixed-length CTA: EPT elements each, a multiple of 32
 __host__ __device__ constexpr int fixed_threads(int L, int log2W, int EPT)
 {
@@ -472,7 +504,62 @@ __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bi
         if (row < a.nrows) v = ld_stream(in + row * a.in_stride + 2 * (crank + (long long)C * m));
         return v;
     };
-    if constexpr (A::kScaled) {
+    if constexpr (kFixed && C == 1) {
+        // first pass fed from global memory: task (jj, w) takes elements
+        // jj + LR1 r of row w into registers (float-float: the row's largest
+        // exponent is reduced from the raw doubles before they are converted)
+        using V2 = typename std::conditional<sizeof(S) == 8, double2, float2>::type;
+        constexpr int NT = fixed_threads(FL, FW, EPT);
+        constexpr int R1 = fixed_radix(FL, 1, EPT), LR1 = FL / R1;
+        constexpr int NTASK = LR1 << FW, TPT = (NTASK + NT - 1) / NT;
+        static_assert(NT % (1 << FW) == 0, "a thread's tasks share one row");
+        const bool active = tid < NT;  // bodies may run in a larger CTA (batch kernel)
+        V2 raw[TPT][R1];
+#pragma unroll
+        for (int t = 0; t < TPT; ++t) {
+            const int task = tid + t * NT;
+            const int w = task & wmask, jj = task >> log2W, row = row0 + w;
+#pragma unroll
+            for (int r = 0; r < R1; ++r) {
+                raw[t][r] = V2{};
+                if (active && (NTASK % NT == 0 || task < NTASK) && row < a.nrows)
+                    raw[t][r] = ld_stream(in + row * a.in_stride + 2 * (long long)(jj + r * LR1));
+            }
+        }
+        if constexpr (A::kScaled) {
+            if (tid < 64) sE[tid] = 0;
+            __syncthreads();
+            int emax = 0;
+#pragma unroll
+            for (int t = 0; t < TPT; ++t)
+#pragma unroll
+                for (int r = 0; r < R1; ++r)
+                    emax = max(emax, max(dbl_biased_exp(raw[t][r].x), dbl_biased_exp(raw[t][r].y)));
+            reduce_exponents<1>(emax, log2W, sE, sEc);
+        }
+#pragma unroll
+        for (int t = 0; t < TPT; ++t) {
+            const int task = tid + t * NT;
+            if (active && (NTASK % NT == 0 || task < NTASK)) {
+                const int w = task & wmask, jj = task >> log2W;
+                cpx<T> v[R1];
+                if constexpr (A::kScaled) {
+                    const int E = scale_exp(sEc[w]);
+#pragma unroll
+                    for (int r = 0; r < R1; ++r)
+                        v[r] = cpx<T>{ff_from_double(raw[t][r].x, E), ff_from_double(raw[t][r].y, E)};
+                } else {
+#pragma unroll
+                    for (int r = 0; r < R1; ++r) v[r] = cpx<T>{(T)raw[t][r].x, (T)raw[t][r].y};
+                }
+                DFT<R1, -1, T>::run(v);
+#pragma unroll
+                for (int r = 0; r < R1; ++r) s[pidx(((jj * R1 + r) << log2W) + w)] = cnorm(v[r]);
+            }
+        }
+        __syncthreads();
+        FixedPassRange<T, FL, (1 << FW), NT, -1, EPT, R1, 0, FL>::run(s, ptab);
+    } else if constexpr (A::kScaled) {
         if (tid < 64) sE[tid] = 0;
         __syncthreads();
         int emax = 0;
@@ -492,10 +579,11 @@ __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bi
         using V2 = typename std::conditional<sizeof(S) == 8, double2, float2>::type;
         batched_loop<EPT, V2>(nel, nth, ld_row, [&](int t, V2 v) { s[pidx(t)] = cpx<T>{(T)v.x, (T)v.y}; });
     }
-    __syncthreads();
-
-    // W_M^(c k2) = W_2M^(2 c k2)
-    local_stage<A, -1, C, FL, FW, A::kScaled>(s, L, log2W, a.pp, tw, a.Ltab, ptab, sEc, 2 * (int)crank);
+    if constexpr (!(kFixed && C == 1)) {
+        __syncthreads();
+        // W_M^(c k2) = W_2M^(2 c k2)
+        local_stage<A, -1, C, FL, FW, A::kScaled>(s, L, log2W, a.pp, tw, a.Ltab, ptab, sEc, 2 * (int)crank);
+    }
 
     if constexpr (C == 1) {
         const int ntask = (M / 2 + 1) << log2W;
@@ -954,38 +1042,6 @@ __global__ void HPXFFT_BOUNDS(A, FL) colstep_kernel(ColStepArgs a)
             store_c<A>(o, v, E);
     }
 }
-
-// Ls of the last pass of the compile-time chain for length L, and the
-// per-pass table offset of the pass at Ls (the layout FixedPasses uses).
-__host__ __device__ constexpr int last_pass_ls(int L, int maxR)
-{
-    int Ls = 1;
-    while (Ls * fixed_radix(L, Ls, maxR) < L) Ls *= fixed_radix(L, Ls, maxR);
-    return Ls;
-}
-__host__ __device__ constexpr int pass_table_offset(int L, int maxR, int upto)
-{
-    int Ls = 1, off = 0;
-    while (Ls < upto) {
-        const int R = fixed_radix(L, Ls, maxR);
-        if (Ls > 1) off += Ls * (R - 1);
-        Ls *= R;
-    }
-    return off;
-}
-
-// The compile-time chain's passes with Ls in [Ls, END), through shared memory.
-template <class T, int L, int W, int NT, int DIR, int MAXR, int Ls, int Off, int END>
-struct FixedPassRange {
-    static __device__ __forceinline__ void run(cpx<T> *s, const cpx<T> *__restrict__ ptab)
-    {
-        if constexpr (Ls < END) {
-            constexpr int R = fixed_radix(L, Ls, MAXR);
-            fixed_pass<T, R, L, W, NT, DIR, Ls, false, false>(s, ptab + Off, nullptr, nullptr, 0);
-            FixedPassRange<T, L, W, NT, DIR, MAXR, Ls * R, Off + Ls * (R - 1), END>::run(s, ptab);
-        }
-    }
-};
 
 // A column step with the first pass fed from global memory and the last
 // pass written to it, so shared memory only carries the transposes between
