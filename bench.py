@@ -469,7 +469,8 @@ def extras(torch, hpxfft, args, x64, oracle_ref, peak):
             sec = {"workload": f"2d_r2c_{prec}_{nx}x{ny}", "ms": ms, "value": B / (ms * 1e-3) / 1e9, "unit": "GB/s",
                    "frac_of_measured_hbm": B / (ms * 1e-3) / 1e9 / peak}
             if prec == "bf16x3":
-                sec["tensor_core_stage"] = "first radix-16 pass of both column steps, tcgen05 kind::f16, 3-term BF16 split"
+                sec["tensor_core_stage"] = ("first radix-16 pass of the rows and of both column steps, tcgen05 "
+                                            "kind::f16, 3-term BF16 split, FP32 accumulate")
             if oracle_ref is not None:
                 got = y32.cpu().numpy().view(np.complex64).astype(np.complex128)
                 d = got - oracle_ref

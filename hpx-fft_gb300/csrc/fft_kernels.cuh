@@ -479,6 +479,38 @@ __device__ __forceinline__ void local_stage(cpx<typename A::T> *s, int L, int lo
 // Replaces the FFTW row pass core/src/shared/loop.cpp:61-69 (fft_1d_r2c_inplace,
 // loop.cpp:6-9); output row kx holds X[kx][0..M] in place of the padded input.
 // Body of the row r2c for row group `group` of batch item `bidx`.
+// Packed-real split of the W transforms Z (length M) in shared memory into
+// X[0..M] of rows row0 + w:  X[k] = E - i W_2M^k O,  X[M-k] = conj(E + i W_2M^k O).
+// Threads t0, t0 + nth, ... take the tasks (t0 past the end: idle).
+template <class A>
+__device__ __forceinline__ void row_r2c_split(const cpx<typename A::T> *s, const RowArgs &a, int row0, int log2W,
+                                              const cpx<typename A::T> *__restrict__ tw, typename A::S *out, int bidx,
+                                              const int *sEc, int t0, int nth)
+{
+    using T = typename A::T;
+    using S = typename A::S;
+    const int M = a.M, wmask = (1 << log2W) - 1;
+    const int ntask = (M / 2 + 1) << log2W;
+    for (int t = t0; t < ntask; t += nth) {
+        const int w = t & wmask, k = t >> log2W, row = row0 + w;
+        if (row >= a.nrows) continue;
+        const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
+        const cpx<T> za = s[pidx((k << log2W) + w)];
+        const cpx<T> zb = cconj(s[pidx((((M - k) % M) << log2W) + w)]);
+        const cpx<T> e = chalf(za + zb), o = chalf(za - zb);
+        const cpx<T> tk = cmul(tw[k], o);
+        S *orow = out + row * a.out_stride;
+        if (A::kScaled && a.pairs_out) {
+            store_pair<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk));
+            if (M - k != k) store_pair<A>(orow + 2 * (long long)(M - k), cconj(e + mul_i<+1>(tk)));
+            if (k == 0) a.exp_out[(long long)bidx * a.nrows + row] = block_exp(sEc[w]);
+            continue;
+        }
+        store_c<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk), E);
+        if (M - k != k) store_c<A>(orow + 2 * (long long)(M - k), cconj(e + mul_i<+1>(tk)), E);
+    }
+}
+
 template <class A, int C, int FL, int FW>
 __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bidx)
 {
@@ -586,25 +618,7 @@ __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bi
     }
 
     if constexpr (C == 1) {
-        const int ntask = (M / 2 + 1) << log2W;
-        for (int t = t0; t < ntask; t += nth) {
-            const int w = t & wmask, k = t >> log2W, row = row0 + w;
-            if (row >= a.nrows) continue;
-            const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
-            const cpx<T> za = s[pidx((k << log2W) + w)];
-            const cpx<T> zb = cconj(s[pidx((((M - k) % M) << log2W) + w)]);
-            const cpx<T> e = chalf(za + zb), o = chalf(za - zb);
-            const cpx<T> tk = cmul(tw[k], o);
-            S *orow = out + row * a.out_stride;
-            if (A::kScaled && a.pairs_out) {
-                store_pair<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk));
-                if (M - k != k) store_pair<A>(orow + 2 * (long long)(M - k), cconj(e + mul_i<+1>(tk)));
-                if (k == 0) a.exp_out[(long long)bidx * a.nrows + row] = block_exp(sEc[w]);
-                continue;
-            }
-            store_c<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk), E);
-            if (M - k != k) store_c<A>(orow + 2 * (long long)(M - k), cconj(e + mul_i<+1>(tk)), E);
-        }
+        row_r2c_split<A>(s, a, row0, log2W, tw, out, bidx, sEc, t0, nth);
     } else {
         cg::cluster_group cl = cg::this_cluster();
         const int E = A::kScaled ? scale_exp(sEc[0]) : 0;
@@ -1043,6 +1057,56 @@ __global__ void HPXFFT_BOUNDS(A, FL) colstep_kernel(ColStepArgs a)
     }
 }
 
+// The last pass of a compile-time column-step chain, from the shared-memory
+// tile to global memory: outputs k = base + r LSL of column col0 + w go to
+// row out_row0 + out_step k, times W_nx^(g k) when the step has a post
+// twiddle.  NT threads (of a possibly larger CTA) share the tasks.
+template <class A, int DIR, int FL, int W, int NT>
+__device__ __forceinline__ void colstep_last_pass_global(const cpx<typename A::T> *s,
+                                                         const cpx<typename A::T> *__restrict__ ptab,
+                                                         const ColStepArgs &a, int g, int col0, typename A::S *out,
+                                                         long long out_row0, int E, bool pairs_out)
+{
+    using T = typename A::T;
+    using S = typename A::S;
+    constexpr int EPT = A::kEPTFixed;
+    constexpr int LSL = last_pass_ls(FL, EPT), RL = fixed_radix(FL, LSL, EPT), LRL = FL / RL;
+    constexpr int Off = pass_table_offset(FL, EPT, LSL);
+    constexpr int NTASK = LRL * W, TPT = (NTASK + NT - 1) / NT;
+    const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
+    const cpx<T> *tp = ptab + Off;
+    const int tid = threadIdx.x;
+    if (tid >= NT) return;
+#pragma unroll
+    for (int t = 0; t < TPT; ++t) {
+        const int task = tid + t * NT;
+        if (NTASK % NT == 0 || task < NTASK) {
+            const int w = task % W, jj = task / W, col = col0 + w;
+            const int k = jj % LSL;
+            cpx<T> v[RL];
+#pragma unroll
+            for (int r = 0; r < RL; ++r) v[r] = s[pidx((jj + r * LRL) * W + w)];
+#pragma unroll
+            for (int r = 1; r < RL; ++r) v[r] = cmul(v[r], twid<DIR>(tp, (r - 1) * LSL + k));
+            DFT<RL, DIR, T>::run(v);
+            if (col < a.ncols) {
+                const int base = (jj - k) * RL + k;
+#pragma unroll
+                for (int r = 0; r < RL; ++r) {
+                    const int kk = base + r * LSL;
+                    cpx<T> o = v[r];
+                    if (a.post && g) o = cmul(o, twid<DIR>(tw, g * kk));
+                    S *dst = out + (out_row0 + (long long)a.out_step * kk) * a.row_stride + 2 * (long long)col;
+                    if (pairs_out)
+                        store_pair<A>(dst, o);
+                    else
+                        store_c<A>(dst, o, E);
+                }
+            }
+        }
+    }
+}
+
 // A column step with the first pass fed from global memory and the last
 // pass written to it, so shared memory only carries the transposes between
 // passes (one round trip for L = 128 in FP32 instead of three).  Same
@@ -1136,40 +1200,8 @@ __global__ void __launch_bounds__(fixed_threads(FL, FW, A::kEPTFixed),
     // last pass: outputs k = base + r LSL go straight to their rows
     const bool pairs_out = A::kScaled && a.pairs_out;
     if (pairs_out && tid == 0) a.exp_out[blockIdx.x + (long long)gridDim.x * blockIdx.y] = Eblk;
-    const int E = Eblk == kExpNone ? 0 : Eblk;
-    {
-        constexpr int Off = pass_table_offset(FL, EPT, LSL);
-        constexpr int NTASK = LRL * W, TPT = (NTASK + NT - 1) / NT;
-        const cpx<T> *tp = ptab + Off;
-#pragma unroll
-        for (int t = 0; t < TPT; ++t) {
-            const int task = tid + t * NT;
-            if (NTASK % NT == 0 || task < NTASK) {
-                const int w = task % W, jj = task / W, col = col0 + w;
-                const int k = jj % LSL;
-                cpx<T> v[RL];
-#pragma unroll
-                for (int r = 0; r < RL; ++r) v[r] = s[pidx((jj + r * LRL) * W + w)];
-#pragma unroll
-                for (int r = 1; r < RL; ++r) v[r] = cmul(v[r], twid<DIR>(tp, (r - 1) * LSL + k));
-                DFT<RL, DIR, T>::run(v);
-                if (col < a.ncols) {
-                    const int base = (jj - k) * RL + k;
-#pragma unroll
-                    for (int r = 0; r < RL; ++r) {
-                        const int kk = base + r * LSL;
-                        cpx<T> o = v[r];
-                        if (a.post && g) o = cmul(o, twid<DIR>(tw, g * kk));
-                        S *dst = out + (out_row0 + (long long)a.out_step * kk) * a.row_stride + 2 * (long long)col;
-                        if (pairs_out)
-                            store_pair<A>(dst, o);
-                        else
-                            store_c<A>(dst, o, E);
-                    }
-                }
-            }
-        }
-    }
+    colstep_last_pass_global<A, DIR, FL, W, NT>(s, ptab, a, g, col0, out, out_row0, Eblk == kExpNone ? 0 : Eblk,
+                                                pairs_out);
 }
 
 // --------------------------------------------------------- twiddle tables

@@ -1,4 +1,4 @@
-// Split-BF16 tensor-core column steps and their DFT-matrix table.
+// Split-BF16 tensor-core column steps, rows and their DFT-matrix table.
 #include "launch.cuh"
 #include "tc_colstep.cuh"
 
@@ -62,6 +62,50 @@ cudaError_t TcColStepLaunch::run(const ColStepArgs &a, const void *dft, int *err
         return cudaGetLastError();                                                                     \
     }
     HPXFFT_TC_SHAPES(HPXFFT_X)
+#undef HPXFFT_X
+    return cudaErrorInvalidValue;
+}
+
+#define HPXFFT_TC_ROWS(X) X(8192, 0) X(4096, 1) X(2048, 2) X(1024, 3) X(512, 4) X(256, 4) X(128, 4)
+
+cudaError_t TcRowLaunch::prepare()
+{
+    cudaError_t e = cudaSuccess;
+#define HPXFFT_X(L, W)                                                                                           \
+    if ((e = cudaFuncSetAttribute(row_r2c_tc_kernel<L, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,          \
+                                  (int)tc_smem(L * (1 << W) / 16))) != cudaSuccess)                               \
+        return e;
+    HPXFFT_TC_ROWS(HPXFFT_X)
+#undef HPXFFT_X
+    return e;
+}
+
+bool TcRowLaunch::supports(int M, int log2W, int C)
+{
+    if (C != 1) return false;
+#define HPXFFT_X(L_, W_) \
+    if (M == L_ && log2W == W_) return true;
+    HPXFFT_TC_ROWS(HPXFFT_X)
+#undef HPXFFT_X
+    return false;
+}
+
+int TcRowLaunch::threads(int M, int log2W) { return (M << log2W) / 16; }
+size_t TcRowLaunch::smem(int M, int log2W) { return tc_smem((M << log2W) / 16); }
+
+cudaError_t TcRowLaunch::run(const RowArgs &a, const void *dft, int *error, dim3 grid, cudaStream_t st)
+{
+    TcRowArgs ta;
+    ta.r = a;
+    ta.dft = dft;
+    ta.error = error;
+    ta.spin_limit = kTcSpinLimit;
+#define HPXFFT_X(L_, W_)                                                                                \
+    if (a.M == L_ && a.log2W == W_) {                                                                   \
+        row_r2c_tc_kernel<L_, W_><<<grid, (L_ << W_) / 16, tc_smem((L_ << W_) / 16), st>>>(ta);         \
+        return cudaGetLastError();                                                                      \
+    }
+    HPXFFT_TC_ROWS(HPXFFT_X)
 #undef HPXFFT_X
     return cudaErrorInvalidValue;
 }

@@ -72,6 +72,16 @@ struct TcColStepLaunch {
     static cudaError_t run(const ColStepArgs &a, const void *dft, int *error, int dir, dim3 grid, cudaStream_t st);
 };
 
+// Split-BF16 row r2c (kernels_tc_cols.cu): compiled (M, log2 rows per CTA)
+// shapes of the FP32 row plan with 128, 256 or 512 length-16 vectors per CTA.
+struct TcRowLaunch {
+    static cudaError_t prepare();
+    static bool supports(int M, int log2W, int C);
+    static int threads(int M, int log2W);
+    static size_t smem(int M, int log2W);
+    static cudaError_t run(const RowArgs &a, const void *dft, int *error, dim3 grid, cudaStream_t st);
+};
+
 template <class A>
 struct TwiddleLaunch {
     static cudaError_t full(void *tab, int n, cudaStream_t st);

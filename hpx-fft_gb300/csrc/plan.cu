@@ -67,8 +67,10 @@ struct hpxfft_plan_s {
     bool ff_pairs = false;
     int *exp_rows = nullptr;   // [batch][nx]
     int *exp_step_a = nullptr; // [batch][step A blocks]
-    // split-BF16 precision: both column steps on the tensor cores
+    // split-BF16 precision: both column steps (and the rows, for compiled
+    // row shapes) on the tensor cores
     bool tc_cols = false;
+    bool tc_rows = false;
     void *tc_dft = nullptr;     // BF16 DFT-16 matrix splits
     int *dev_error = nullptr;   // set by a tensor-core kernel whose wait gave up
     void *tw_row = nullptr, *tw_col = nullptr;
@@ -334,6 +336,7 @@ static cudaError_t prepare_tc_once()
     std::lock_guard<std::mutex> lock(mu);
     if (done[dev]) return cudaSuccess;
     e = TcColStepLaunch::prepare();
+    if (e == cudaSuccess) e = TcRowLaunch::prepare();
     if (e == cudaSuccess) done[dev] = true;
     return e;
 }
@@ -531,7 +534,11 @@ static cudaError_t run_forward(hpxfft_plan_s &p, const void *in, void *out, void
         ra.pairs_out = 1;
         ra.exp_out = p.exp_rows;
     }
-    if ((e = RowLaunch<A>::r2c(ra, p.row.shape, p.row.FL, p.stream)) != cudaSuccess) return e;
+    if (p.tc_rows)
+        e = TcRowLaunch::run(ra, p.tc_dft, p.dev_error, p.row.shape.grid, p.stream);
+    else
+        e = RowLaunch<A>::r2c(ra, p.row.shape, p.row.FL, p.stream);
+    if (e != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
     void *dst = final_out && p.col_two_step ? final_out : out;
     if ((e = run_columns<A>(p, out, -1, dst)) != cudaSuccess) return e;
@@ -640,7 +647,7 @@ static std::string describe(const hpxfft_plan_s &p, const DimPlan &d, const char
              d.shape.grid.y, d.shape.threads, d.shape.smem,
              p.prec == HPXFFT_PREC_F64          ? "f64-floatfloat"
              : p.prec == HPXFFT_PREC_F64_NATIVE ? "f64-dfma"
-             : p.prec == HPXFFT_PREC_BF16X3     ? (p.tc_cols && &d != &p.row ? "bf16x3-tcgen05" : "f32")
+             : p.prec == HPXFFT_PREC_BF16X3     ? ((&d == &p.row ? p.tc_rows : p.tc_cols) ? "bf16x3-tcgen05" : "f32")
                                                 : "f32");
     return buf;
 }
@@ -753,6 +760,17 @@ int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
                 rc = cuda_fail(e, "tensor-core tables");
             } else {
                 p->tc_cols = true;
+                // rows: the tensor-core r2c where the FP32 plan has a compiled
+                // single-CTA shape of 128..512 vectors; other rows stay FP32
+                // (the launcher sizes its own CTAs; row.shape stays the FP32
+                // one, which the inverse's c2r rows use).  HPXFFT_TC_ROWS=0
+                // keeps FP32 rows (16384^2: 0.61 ms against 0.93 ms for the
+                // tensor-core row, whose BF16 split costs more CUDA-core
+                // work than the radix-16 butterfly it replaces)
+                const char *rows_env = std::getenv("HPXFFT_TC_ROWS");
+                if (p->row.FL && TcRowLaunch::supports((int)p->M, p->row.log2W, p->row.C) &&
+                    !(rows_env && !strcmp(rows_env, "0")))
+                    p->tc_rows = true;
             }
         }
     }

@@ -71,57 +71,41 @@ __device__ __forceinline__ void split3_bf16(const float (&v)[8], uint4 &h, uint4
     l = make_uint4(pl[0], pl[1], pl[2], pl[3]);
 }
 
-template <int DIR, int FL, int NV>
-__global__ void __launch_bounds__(NV, 2 * 512 / NV) colstep_tc_kernel(TcColStepArgs ta)
+// ---- the tensor-core DFT-16 stage, shared by the column-step and row kernels
+
+// Tensor memory for the accumulators (warp 0), the MMA barrier (thread 0)
+// and the DFT matrix of direction dir into sB.  The caller's next CTA barrier
+// (inside tc_dft16) publishes all three.
+template <int NV>
+__device__ __forceinline__ void tc_setup(uint32_t *tmem_slot, uint64_t *bar, unsigned char *sB, const void *dft,
+                                         int dir)
 {
-    constexpr int kTcThreads = NV;
-    constexpr int kTcBlocks = NV / 128;
-    constexpr int kTcABytes = tc_a_bytes(NV);
-    constexpr int kTcTmemCols = tc_tmem_cols(NV);
-    constexpr int LR = FL / 16;                // vectors per column
-    constexpr int W = NV / LR;                 // columns per CTA
-    constexpr int log2W = ilog2c(W);
-    constexpr int nel = FL * W;
-    static_assert(FL % 16 == 0 && (1 << log2W) == W, "length must be 16 times a power of two");
-    const ColStepArgs &a = ta.c;
-    extern __shared__ unsigned char smem_raw[];
-    __shared__ uint64_t s_bar;
-    __shared__ uint32_t s_tmem;
-    unsigned char *base = smem_raw + ((128 - (tc::smem_addr(smem_raw) & 127)) & 127);
-    unsigned char *sA = base;
-    unsigned char *sB = base + kTcABytes;
-    cpx<float> *s = reinterpret_cast<cpx<float> *>(base);  // FP32 tile once the MMAs are done
-
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const int g = blockIdx.x / a.strips, col0 = (blockIdx.x % a.strips) * W;
-    const float *in = reinterpret_cast<const float *>(a.in) + (long long)blockIdx.y * a.in_bstride;
-    float *out = reinterpret_cast<float *>(a.out) + (long long)blockIdx.y * a.out_bstride;
-    const cpx<float> *tw = reinterpret_cast<const cpx<float> *>(a.tw);
-    const cpx<float> *ptab = reinterpret_cast<const cpx<float> *>(a.ptab);
-    const long long in_row0 = (long long)g * a.in_gmul, out_row0 = (long long)g * a.out_gmul;
-
-    if (warp == 0) {
-        tc::tmem_alloc(&s_tmem, kTcTmemCols);
+    const int tid = threadIdx.x;
+    if ((tid >> 5) == 0) {
+        tc::tmem_alloc(tmem_slot, tc_tmem_cols(NV));
         tc::tmem_relinquish();
     }
     if (tid == 0) {
-        tc::mbar_init(&s_bar, 1);
+        tc::mbar_init(bar, 1);
         tc::fence_mbar_init();
     }
-    {
-        const uint4 *src = reinterpret_cast<const uint4 *>(ta.dft) + (DIR < 0 ? 0 : kTcBBytes / 16);
-        for (int i = tid; i < kTcBBytes / 16; i += kTcThreads) reinterpret_cast<uint4 *>(sB)[i] = src[i];
-    }
+    const uint4 *src = reinterpret_cast<const uint4 *>(dft) + (dir < 0 ? 0 : kTcBBytes / 16);
+    for (int i = tid; i < kTcBBytes / 16; i += NV) reinterpret_cast<uint4 *>(sB)[i] = src[i];
+}
 
-    // this thread's vector: column w, elements jj + LR t
-    const int jj = tid >> log2W, w = tid & (W - 1), col = col0 + w;
+// DFT-16 of the CTA's NV vectors, one per thread: x = the thread's 16
+// inputs, y = its 16 outputs (Re X_0..15, Im X_0..15).  Contains the CTA
+// barriers.  Returns false in every thread if the MMA wait gave up (after
+// flagging *error and waiting once more, bounded); on true the operand
+// space is free again.
+template <int NV>
+__device__ __forceinline__ bool tc_dft16(const float2 (&x)[16], float (&y)[32], unsigned char *sA,
+                                         const unsigned char *sB, const uint32_t *tmem_slot, uint64_t *bar,
+                                         int *error, long long spin_limit)
+{
+    constexpr int kTcBlocks = NV / 128;
+    const int tid = threadIdx.x, warp = tid >> 5;
     {
-        float2 x[16];
-        const bool live = col < a.ncols;
-        const float *src = in + (in_row0 + (long long)a.in_step * jj) * a.row_stride + 2 * (long long)col;
-        const long long tstride = (long long)a.in_step * LR * a.row_stride;
-#pragma unroll
-        for (int t = 0; t < 16; ++t) x[t] = live ? ld_stream(src + t * tstride) : make_float2(0.f, 0.f);
         // operand row tid & 127 of block tid >> 7; K chunks 0, 1: real parts, 2, 3: imaginary parts
         unsigned char *arow = sA + (tid >> 7) * 3 * kTcOperandBytes;
         const int row = tid & 127;
@@ -142,7 +126,7 @@ __global__ void __launch_bounds__(NV, 2 * 512 / NV) colstep_tc_kernel(TcColStepA
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tmem = s_tmem;
+    const uint32_t tmem = *tmem_slot;
 
     if (tid == 0) {
         constexpr uint32_t idesc = tc::idesc_bf16_f32(128, 32);
@@ -161,12 +145,12 @@ __global__ void __launch_bounds__(NV, 2 * 512 / NV) colstep_tc_kernel(TcColStepA
                 }
             }
         }
-        tc::mma_commit(&s_bar);
+        tc::mma_commit(bar);
     }
 
     int ok = 1;
-    for (long long spins = 0; !tc::mbar_try_wait(&s_bar, 0);) {
-        if (++spins > ta.spin_limit) {
+    for (long long spins = 0; !tc::mbar_try_wait(bar, 0);) {
+        if (++spins > spin_limit) {
             ok = 0;
             break;
         }
@@ -175,34 +159,126 @@ __global__ void __launch_bounds__(NV, 2 * 512 / NV) colstep_tc_kernel(TcColStepA
     tc::fence_after_sync();
     if (all_ok) {
         // warp w reads TMEM lanes 32 (w % 4).. of block w / 4: row tid & 127 of block tid >> 7, its own vector
-        float r[32];
-        tc::tmem_ld_32x32b_x32(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(32 * (warp >> 2)), r);
-        // Stockham order after the first radix-16 pass: output q of vector jj at element 16 jj + q
-#pragma unroll
-        for (int q = 0; q < 16; ++q) s[pidx(((16 * jj + q) << log2W) + w)] = cpx<float>{r[q], r[16 + q]};
+        tc::tmem_ld_32x32b_x32(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(32 * (warp >> 2)), y);
     } else if (tid == 0) {
-        atomicExch(ta.error, 1);
+        atomicExch(error, 1);
         // one more bounded wait for the MMAs in flight before their TMEM is freed
-        for (long long spins = 0; !tc::mbar_try_wait(&s_bar, 0) && spins < ta.spin_limit; ++spins) {
+        for (long long spins = 0; !tc::mbar_try_wait(bar, 0) && spins < spin_limit; ++spins) {
         }
     }
+    return all_ok != 0;
+}
+
+// Free the tensor memory once every thread's loads from it are done.
+template <int NV>
+__device__ __forceinline__ void tc_teardown(const uint32_t *tmem_slot)
+{
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) {
+    if ((threadIdx.x >> 5) == 0) {
         tc::fence_after_sync();
-        tc::tmem_dealloc(tmem, kTcTmemCols);
+        tc::tmem_dealloc(*tmem_slot, tc_tmem_cols(NV));
     }
-    if (!all_ok) return;
+}
 
-    FixedPasses<float, FL, W, kTcThreads, DIR, 16, 16, 0, false, false>::run(s, ptab, nullptr, tw, 0);
+template <int DIR, int FL, int NV>
+__global__ void __launch_bounds__(NV, 2 * 512 / NV) colstep_tc_kernel(TcColStepArgs ta)
+{
+    constexpr int LR = FL / 16;                // vectors per column
+    constexpr int W = NV / LR;                 // columns per CTA
+    constexpr int log2W = ilog2c(W);
+    static_assert(FL % 16 == 0 && (1 << log2W) == W, "length must be 16 times a power of two");
+    const ColStepArgs &a = ta.c;
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ uint64_t s_bar;
+    __shared__ uint32_t s_tmem;
+    unsigned char *base = smem_raw + ((128 - (tc::smem_addr(smem_raw) & 127)) & 127);
+    unsigned char *sA = base;
+    unsigned char *sB = base + tc_a_bytes(NV);
+    cpx<float> *s = reinterpret_cast<cpx<float> *>(base);  // FP32 tile once the MMAs are done
 
-    for (int t = tid; t < nel; t += kTcThreads) {
-        const int ww = t & (W - 1), k = t >> log2W, c = col0 + ww;
-        if (c >= a.ncols) continue;
-        cpx<float> v = s[pidx(t)];
-        if (a.post && g) v = cmul(v, twid<DIR>(tw, g * k));
-        store_c<ArithF32>(out + (out_row0 + (long long)a.out_step * k) * a.row_stride + 2 * (long long)c, v, 0);
+    const int tid = threadIdx.x;
+    const int g = blockIdx.x / a.strips, col0 = (blockIdx.x % a.strips) * W;
+    const float *in = reinterpret_cast<const float *>(a.in) + (long long)blockIdx.y * a.in_bstride;
+    float *out = reinterpret_cast<float *>(a.out) + (long long)blockIdx.y * a.out_bstride;
+    const cpx<float> *ptab = reinterpret_cast<const cpx<float> *>(a.ptab);
+    const long long in_row0 = (long long)g * a.in_gmul, out_row0 = (long long)g * a.out_gmul;
+
+    tc_setup<NV>(&s_tmem, &s_bar, sB, ta.dft, DIR);
+    // this thread's vector: column w, elements jj + LR t
+    const int jj = tid >> log2W, w = tid & (W - 1), col = col0 + w;
+    float2 x[16];
+    {
+        const bool live = col < a.ncols;
+        const float *src = in + (in_row0 + (long long)a.in_step * jj) * a.row_stride + 2 * (long long)col;
+        const long long tstride = (long long)a.in_step * LR * a.row_stride;
+#pragma unroll
+        for (int t = 0; t < 16; ++t) x[t] = live ? ld_stream(src + t * tstride) : make_float2(0.f, 0.f);
     }
+    float y[32];
+    const bool ok = tc_dft16<NV>(x, y, sA, sB, &s_tmem, &s_bar, ta.error, ta.spin_limit);
+    if (ok)  // Stockham order after the first radix-16 pass: output q of vector jj at element 16 jj + q
+#pragma unroll
+        for (int q = 0; q < 16; ++q) s[pidx(((16 * jj + q) << log2W) + w)] = cpx<float>{y[q], y[16 + q]};
+    tc_teardown<NV>(&s_tmem);
+    if (!ok) return;
+
+    // remaining FP32 passes; the last one writes its rows directly
+    FixedPassRange<float, FL, W, NV, DIR, 16, 16, 0, last_pass_ls(FL, 16)>::run(s, ptab);
+    colstep_last_pass_global<ArithF32, DIR, FL, W, NV>(s, ptab, a, g, col0, out, out_row0, 0, false);
+}
+
+// Row r2c with the first radix-16 pass on the tensor cores: W rows of M = FL
+// packed-real points per CTA (NV = FL W / 16 vectors, one per thread; vector
+// (jj, w) = z[jj + (FL/16) t] of row w), then the FP32 passes and the
+// packed-real split, as row_r2c_kernel.
+struct TcRowArgs {
+    RowArgs r;
+    const void *dft;
+    int *error;
+    long long spin_limit;
+};
+
+template <int FL, int FW>
+__global__ void __launch_bounds__(FL * (1 << FW) / 16, 1024 / (FL * (1 << FW) / 16)) row_r2c_tc_kernel(TcRowArgs ta)
+{
+    constexpr int W = 1 << FW, NV = FL * W / 16, LR = FL / 16;
+    static_assert(NV == 128 || NV == 256 || NV == 512, "128, 256 or 512 vectors per CTA");
+    static_assert(FL >= 32, "a pass after the tensor-core one");
+    const RowArgs &a = ta.r;
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ uint64_t s_bar;
+    __shared__ uint32_t s_tmem;
+    unsigned char *base = smem_raw + ((128 - (tc::smem_addr(smem_raw) & 127)) & 127);
+    unsigned char *sA = base;
+    unsigned char *sB = base + tc_a_bytes(NV);
+    cpx<float> *s = reinterpret_cast<cpx<float> *>(base);
+
+    const int tid = threadIdx.x, bidx = blockIdx.y, row0 = blockIdx.x * W;
+    const float *in = reinterpret_cast<const float *>(a.in) + (long long)bidx * a.in_bstride;
+    float *out = reinterpret_cast<float *>(a.out) + (long long)bidx * a.out_bstride;
+    const cpx<float> *tw = reinterpret_cast<const cpx<float> *>(a.tw);
+    const cpx<float> *ptab = reinterpret_cast<const cpx<float> *>(a.ptab);
+
+    tc_setup<NV>(&s_tmem, &s_bar, sB, ta.dft, -1);
+    const int jj = tid >> FW, w = tid & (W - 1), row = row0 + w;
+    float2 x[16];
+    {
+        const bool live = row < a.nrows;
+        const float *src = in + (long long)row * a.in_stride + 2 * (long long)jj;
+#pragma unroll
+        for (int t = 0; t < 16; ++t) x[t] = live ? ld_stream(src + 2 * (long long)LR * t) : make_float2(0.f, 0.f);
+    }
+    float y[32];
+    const bool ok = tc_dft16<NV>(x, y, sA, sB, &s_tmem, &s_bar, ta.error, ta.spin_limit);
+    if (ok)
+#pragma unroll
+        for (int q = 0; q < 16; ++q) s[pidx(((16 * jj + q) << FW) + w)] = cpx<float>{y[q], y[16 + q]};
+    tc_teardown<NV>(&s_tmem);
+    if (!ok) return;
+
+    FixedPassRange<float, FL, W, NV, -1, 16, 16, 0, FL>::run(s, ptab);
+    row_r2c_split<ArithF32>(s, a, row0, FW, tw, out, bidx, nullptr, tid, NV);
 }
 
 // The three BF16 splits of the real DFT-16 matrix B (K-major: row n of the

@@ -19,8 +19,9 @@
  * is ~1e-14); HPXFFT_PREC_F64_NATIVE computes with DFMA (slow on GB300,
  * kept as a cross-check); HPXFFT_PREC_F32 stores and computes float;
  * HPXFFT_PREC_BF16X3 stores float and runs the first radix-16 stage of each
- * column DFT as a dense complex matmul on the tensor cores (tcgen05, BF16
- * operands split three ways, FP32 accumulation), the other stages in FP32.
+ * column DFT and of each row DFT (compiled row lengths 128..8192) as a dense
+ * complex matmul on the tensor cores (tcgen05, BF16 operands split three
+ * ways, FP32 accumulation), the other stages in FP32.
  */
 #ifndef HPXFFT_GB300_H
 #define HPXFFT_GB300_H

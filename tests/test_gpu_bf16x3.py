@@ -109,3 +109,21 @@ def test_half_occupancy_variant(gpu_lib, cuda, oracle_lib, monkeypatch, nx, ny):
     x = np.random.default_rng(nx - ny).uniform(-1, 1, (nx, ny)).astype(np.float32)
     got = forward(gpu_lib, cuda, x)
     assert rel_l2(got, oracle_fwd(oracle_lib, x.astype(np.float64))) <= TOL, (nx, ny)
+
+
+# every compiled tensor-core row shape: M = ny / 2 in 128 .. 8192
+@pytest.mark.parametrize("ny", [256, 512, 1024, 2048, 4096, 8192, 16384])
+def test_tensor_core_rows_vs_oracle(gpu_lib, cuda, oracle_lib, tmp_path, ny):
+    nx = 1024
+    with gpu_lib.Plan(nx, 2 * (ny // 2 + 1), 1, "bf16x3", "estimate") as plan:
+        plan.write_plan(tmp_path / "plan.txt")
+    first = (tmp_path / "plan.txt").read_text().split("GPU c2c")[0]
+    assert "bf16x3-tcgen05" in first, first
+    x = np.random.default_rng(ny).uniform(-1, 1, (nx, ny)).astype(np.float32)
+    got = forward(gpu_lib, cuda, x)
+    assert rel_l2(got, oracle_fwd(oracle_lib, x.astype(np.float64))) <= TOL, ny
+    # the c2r rows of the inverse stay FP32 on the same plan shape
+    with gpu_lib.Plan(nx, 2 * (ny // 2 + 1), 1, "bf16x3", "estimate") as plan:
+        spec = run_device(cuda, plan, padded(x, np.float32), "forward")
+        back = run_device(cuda, plan, spec, "c2r")
+    assert rel_l2(back[:, :ny] / (nx * ny), x) <= 1e-6
