@@ -85,6 +85,7 @@ struct hpxfft_plan_s {
     cudaEvent_t ev_copy[2] = {};  // before the host->device copy, after the device->host copy
     bool pending_copy = false;
     bool last_zero_copy = false;  // the last host-buffer transform read and wrote host memory directly
+    double peak_gbps = 0.0;       // nominal DRAM bandwidth of the device (memory clock x bus width)
     double sum_first = 0, sum_second = 0, sum_total = 0, sum_step_a = 0;
     long long nsum = 0;
     std::map<std::string, double> meas;
@@ -613,6 +614,9 @@ static int collect(hpxfft_plan_s &p)
         p.meas["total"] = 1e-3 * c;
         const double bytes = 4.0 * (double)(p.nx * p.dcy * 2 * p.real_bytes) * (double)p.batch;
         p.meas["gbps"] = c > 0 ? bytes / (1e-3 * c) / 1e9 : 0.0;
+        const double n = (double)p.nx * (double)p.ny;
+        p.meas["gflops"] = c > 0 && n > 1 ? 2.5 * n * std::log2(n) * (double)p.batch / (1e-3 * c) / 1e9 : 0.0;
+        p.meas["roofline"] = p.peak_gbps > 0 ? p.meas["gbps"] / p.peak_gbps : 0.0;
         if (p.done + 1 == p.next && p.pending_copy) {
             float h = 0, d = 0, t = 0;
             cudaEventElapsedTime(&h, p.ev_copy[0], ev[0]);
@@ -810,6 +814,14 @@ int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
         hpxfft_plan_destroy(p);
         return cuda_fail(e, "twiddle generation");
     }
+    {
+        int dev = 0, clock_khz = 0, bus_bits = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&clock_khz, cudaDevAttrMemoryClockRate, dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&bus_bits, cudaDevAttrGlobalMemoryBusWidth, dev) == cudaSuccess)
+            p->peak_gbps = 2.0 * clock_khz * 1e3 * (bus_bits / 8.0) / 1e9;  // double data rate
+        cudaGetLastError();
+    }
     const auto t1 = std::chrono::steady_clock::now();
     p->meas["plan"] = std::chrono::duration<double>(t1 - t0).count();
     // loop.cpp:188 counts dim_r_y r2c plans and dim_c_x c2c plans; keep that
@@ -976,6 +988,25 @@ int hpxfft_execute_r2c_backward(hpxfft_plan p, void *d)
     cudaError_t e = dispatch_inverse(*p, d, 1);
     if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
     return HPXFFT_OK;
+}
+
+int hpxfft_execute_r2c_backward_host(hpxfft_plan p, void *h)
+{
+    if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
+    if (!h) return fail(HPXFFT_ERR_INVALID_ARG, "null host buffer");
+    int rc = ensure_dbuf(p);
+    if (rc) return rc;
+    const size_t bytes = p->nx * p->ncol * p->real_bytes * p->batch;
+    cudaError_t e;
+    if ((rc = collect(*p)) != HPXFFT_OK) return rc;
+    if ((e = cudaMemcpyAsync(p->dbuf, h, bytes, cudaMemcpyHostToDevice, p->stream)) != cudaSuccess)
+        return cuda_fail(e, "host to device copy");
+    if ((e = dispatch_inverse(*p, p->dbuf, 1)) != cudaSuccess) return cuda_fail(e, "adjoint launch");
+    if ((e = cudaMemcpyAsync(h, p->dbuf, bytes, cudaMemcpyDeviceToHost, p->stream)) != cudaSuccess)
+        return cuda_fail(e, "device to host copy");
+    if ((e = cudaStreamSynchronize(p->stream)) != cudaSuccess) return cuda_fail(e, "adjoint");
+    if ((rc = collect(*p)) != HPXFFT_OK) return rc;
+    return check_device_error(p);
 }
 
 int hpxfft_get_measurement(hpxfft_plan p, const char *name, double *value)

@@ -30,7 +30,16 @@ inline void validate_plan_flag(const std::string &flag)
     if (!hpxfft_plan_flag_valid(flag.c_str())) throw std::invalid_argument("Invalid FFTW plan flag string");
 }
 
+// Precision of the plan for element type T: FP64 (float-float) for double,
+// FP32 for float; PREC overrides it (HPXFFT_PREC_BF16X3 for float buffers,
+// HPXFFT_PREC_F64_NATIVE for double ones).
 template <typename T>
+constexpr int default_precision()
+{
+    return sizeof(T) == 4 ? HPXFFT_PREC_F32 : HPXFFT_PREC_F64;
+}
+
+template <typename T, int PREC = default_precision<T>()>
 class gpu_transform {
   public:
     using vector_type = vector_2d<T>;
@@ -46,8 +55,11 @@ class gpu_transform {
     {
         validate_plan_flag(plan_flag);
         reset();
-        const int prec = sizeof(T) == 4 ? HPXFFT_PREC_F32 : HPXFFT_PREC_F64;
-        check_status(hpxfft_plan_create(&plan_, values_vec.n_row(), values_vec.n_col(), 1, prec, plan_flag.c_str()));
+        static_assert((sizeof(T) == 4) == (PREC == HPXFFT_PREC_F32 || PREC == HPXFFT_PREC_BF16X3),
+                      "float buffers need an FP32-storage precision, double buffers an FP64 one");
+        check_status(hpxfft_plan_create(&plan_, values_vec.n_row(), values_vec.n_col(), 1, PREC, plan_flag.c_str()));
+        n_row_ = values_vec.n_row();
+        n_col_ = values_vec.n_col();
         values_ = std::move(values_vec);
         for (const char *k : {"plan", "plan_flops"}) {
             double v = 0.0;
@@ -61,12 +73,21 @@ class gpu_transform {
     {
         if (!plan_) throw std::runtime_error("initialize() must be called before the transform");
         check_status(hpxfft_execute_r2c_host(plan_, values_.data()));
-        for (const char *k : {"total", "first_fftw", "first_trans", "second_fftw", "second_trans", "h2d", "d2h"}) {
-            double v = 0.0;
-            hpxfft_get_measurement(plan_, k, &v);
-            measurements_[k] = v;
-        }
+        read_measurements();
         return std::move(values_);
+    }
+
+    // gradient of a loss of the spectrum: grad holds dL/dRe X + i dL/dIm X in
+    // the output layout; returns dL/dx in the input layout (pads 0).  The
+    // plan stays usable; no reference counterpart.
+    vector_type run_backward(vector_type grad)
+    {
+        if (!plan_) throw std::runtime_error("initialize() must be called before the transform");
+        if (grad.n_row() != n_row_ || grad.n_col() != n_col_)
+            throw std::invalid_argument("gradient must have the planned n_row x n_col layout");
+        check_status(hpxfft_execute_r2c_backward_host(plan_, grad.data()));
+        read_measurements();
+        return grad;
     }
 
     double measurement(const std::string &name) { return measurements_[name]; }
@@ -82,12 +103,22 @@ class gpu_transform {
     std::map<std::string, double> &measurements() { return measurements_; }
 
   private:
+    void read_measurements()
+    {
+        for (const char *k : {"total", "first_fftw", "first_trans", "second_fftw", "second_trans", "h2d", "d2h", "e2e",
+                              "gbps", "gflops", "roofline"}) {
+            double v = 0.0;
+            hpxfft_get_measurement(plan_, k, &v);
+            measurements_[k] = v;
+        }
+    }
     void reset()
     {
         if (plan_) hpxfft_plan_destroy(plan_);
         plan_ = nullptr;
     }
     hpxfft_plan plan_ = nullptr;
+    std::size_t n_row_ = 0, n_col_ = 0;
     vector_type values_;
     std::map<std::string, double> measurements_;
 };

@@ -58,6 +58,7 @@ SIGNATURES = {
     "hpxfft_batch_execute": (_ci, [_vp, _vp]),
     "hpxfft_batch_synchronize": (_ci, [_vp]),
     "hpxfft_plan_synchronize": (_ci, [_vp]),
+    "hpxfft_execute_r2c_backward_host": (_ci, [_vp, _vp]),
     "hpxfft_batch_get_measurement": (_ci, [_vp, _cs, ctypes.POINTER(ctypes.c_double)]),
     "hpxfft_wisdom_export": (_ci, [_cs]),
     "hpxfft_wisdom_import": (_ci, [_cs]),

@@ -95,6 +95,12 @@ class Plan:
         _capi.check(self._lib.hpxfft_execute_r2c_host(self.handle, values.ctypes.data_as(ctypes.c_void_p)))
         return values
 
+    def backward_host(self, values: np.ndarray) -> np.ndarray:
+        """In-place adjoint of a host array (copy in, transform, copy out)."""
+        self._check_host(values)
+        _capi.check(self._lib.hpxfft_execute_r2c_backward_host(self.handle, values.ctypes.data_as(ctypes.c_void_p)))
+        return values
+
     def _check_host(self, values: np.ndarray) -> None:
         if not isinstance(values, np.ndarray) or not values.flags.c_contiguous:
             raise _capi.HpxFftInvalidArgument(_capi.HPXFFT_ERR_INVALID_ARG, "need a C-contiguous numpy array")

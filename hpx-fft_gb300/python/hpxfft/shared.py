@@ -41,9 +41,24 @@ class _Base:
             raise _capi.HpxFftError(_capi.HPXFFT_ERR_STATE, "initialize() must come first")
         a = self._values
         self._plan.execute_host(a)
-        for key in ("total", "first_fftw", "first_trans", "second_fftw", "second_trans", "h2d", "d2h"):
-            self._meas[key] = self._plan.measurement(key)
+        self._read_measurements()
         self._values = None  # moved out (loop.cpp:112)
+        return vector_2d.from_array(a)
+
+    def _read_measurements(self) -> None:
+        for key in ("total", "first_fftw", "first_trans", "second_fftw", "second_trans", "h2d", "d2h", "e2e",
+                    "gbps", "gflops", "roofline"):
+            self._meas[key] = self._plan.measurement(key)
+
+    def fft_2d_r2c_backward(self, grad: vector_2d) -> vector_2d:
+        """Adjoint of the transform: grad holds dL/dRe X + i dL/dIm X in the
+        output layout; returns dL/dx in the input layout.  No reference
+        counterpart."""
+        if self._plan is None:
+            raise _capi.HpxFftError(_capi.HPXFFT_ERR_STATE, "initialize() must come first")
+        a = np.ascontiguousarray(grad.data(), dtype=self._plan.dtype).reshape(self._plan.n_row, self._plan.n_col).copy()
+        self._plan.backward_host(a)
+        self._read_measurements()
         return vector_2d.from_array(a)
 
     def get_measurement(self, name: str) -> float:

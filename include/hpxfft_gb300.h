@@ -108,6 +108,11 @@ HPXFFT_API int hpxfft_execute_c2r(hpxfft_plan plan, void *device_values);
  * No reference counterpart (gradient for fft_2d_r2c_backward). */
 HPXFFT_API int hpxfft_execute_r2c_backward(hpxfft_plan plan, void *device_values);
 
+/* The adjoint on a host buffer, in place: copies to the plan-owned device
+ * buffer, transforms, copies back, synchronises (the host-side
+ * fft_2d_r2c_backward of the C++ classes).  No reference counterpart. */
+HPXFFT_API int hpxfft_execute_r2c_backward_host(hpxfft_plan plan, void *host_values);
+
 /* Wait for every transform issued on the plan's stream; HPXFFT_ERR_TIMEOUT
  * if a bounded device-side wait of a tensor-core kernel gave up (the flag is
  * cleared by the call).  No reference counterpart (FFTW calls return when
@@ -117,7 +122,10 @@ HPXFFT_API int hpxfft_plan_synchronize(hpxfft_plan plan);
 /* Measurement by key, seconds unless stated: "total", "first_fftw" (row
  * kernel), "first_trans" (0: fused), "second_fftw" (column kernel),
  * "second_trans" (0: fused), "plan", "plan_flops", "h2d", "d2h", "e2e"
- * (host buffer in to host buffer out of the last hpxfft_execute_r2c_host).
+ * (host buffer in to host buffer out of the last hpxfft_execute_r2c_host),
+ * "gbps" (4 S / total, GB/s), "gflops" (2.5 N log2 N per array, N = nx ny,
+ * times batch, / total), "roofline" (gbps over the device's nominal DRAM
+ * bandwidth from its memory clock and bus width, 0 if unknown).
  * Unknown keys give 0, like loop::get_measurement (core/src/shared/loop.cpp:192). */
 HPXFFT_API int hpxfft_get_measurement(hpxfft_plan plan, const char *name, double *value);
 

@@ -3,6 +3,7 @@
 // is the 4 x 6 fixture with rows [1,2,3,4,pad,pad]: initialize(std::move(values),
 // plan) -> transform -> REQUIRE(total >= 0) and REQUIRE(out == expected).
 // Exit status 0 when every check passes.
+#include <cmath>
 #include <cstdio>
 #include <stdexcept>
 #include <string>
@@ -101,6 +102,56 @@ int main()
         vector_2d out = fft.fft_2d_r2c();
         REQUIRE(fft.get_measurement("total") >= 0.0);
         REQUIRE(out == expected());
+    }
+    // precision variants: FP32 on the fixture, split-BF16 on the ramp
+    // x[i][j] = j (closed form), and the adjoint of an impulse at DC
+    {
+        hpxfft::shared::loop_f32 f;
+        hpxfft::util::vector_2d<float> v(4, 6, 0.0f);
+        for (std::size_t i = 0; i < 4; ++i)
+            for (std::size_t j = 0; j < 4; ++j) v(i, j) = (float)(j + 1);
+        f.initialize(std::move(v), "estimate");
+        hpxfft::util::vector_2d<float> out = f.fft_2d_r2c();
+        REQUIRE(out(0, 0) == 40.0f && out(0, 2) == -8.0f && out(0, 3) == 8.0f && out(0, 4) == -8.0f);
+        REQUIRE(f.get_measurement("gbps") >= 0.0);
+    }
+    {
+        const std::size_t nx = 1024, ny = 16, nc = 2 * (ny / 2 + 1);
+        hpxfft::shared::loop_bf16x3 f;
+        hpxfft::util::vector_2d<float> v(nx, nc, 0.0f);
+        for (std::size_t i = 0; i < nx; ++i)
+            for (std::size_t j = 0; j < ny; ++j) v(i, j) = (float)j;
+        f.initialize(std::move(v), "estimate");
+        hpxfft::util::vector_2d<float> out = f.fft_2d_r2c();
+        double err = 0.0, norm = 0.0;
+        const double pi = 3.14159265358979323846;
+        for (std::size_t kx = 0; kx < nx; ++kx)
+            for (std::size_t k = 0; k <= ny / 2; ++k) {
+                double re = 0.0, im = 0.0;
+                if (kx == 0 && k == 0) re = nx * ny * (ny - 1) / 2.0;
+                if (kx == 0 && k > 0) {  // nx ny / (exp(-2 pi i k / ny) - 1)
+                    const double c = std::cos(2 * pi * k / ny) - 1.0, s = -std::sin(2 * pi * k / ny);
+                    const double d = c * c + s * s;
+                    re = nx * ny * c / d;
+                    im = -(double)nx * ny * s / d;
+                }
+                const double dr = out(kx, 2 * k) - re, di = out(kx, 2 * k + 1) - im;
+                err += dr * dr + di * di;
+                norm += re * re + im * im;
+            }
+        REQUIRE(std::sqrt(err / norm) <= 2e-6);
+    }
+    {
+        hpxfft::shared::loop f;
+        f.initialize(input(), "estimate");
+        vector_2d g(4, 6, 0.0);
+        g(0, 0) = 1.0;  // L = Re X[0][0] = sum of the inputs
+        vector_2d grad = f.fft_2d_r2c_backward(std::move(g));
+        bool ones = true;
+        for (std::size_t i = 0; i < 4; ++i)
+            for (std::size_t j = 0; j < 6; ++j) ones = ones && std::fabs(grad(i, j) - (j < 4 ? 1.0 : 0.0)) < 1e-14;
+        REQUIRE(ones);
+        REQUIRE(f.fft_2d_r2c() == expected());  // the plan stays usable
     }
     // error behaviour
     {

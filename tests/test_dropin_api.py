@@ -66,6 +66,8 @@ def test_measurement_keys_and_plan_file(gpu_lib, cuda, tmp_path):
     for key in ("total", "first_fftw", "second_fftw", "plan", "plan_flops", "h2d", "d2h"):
         assert fft.get_measurement(key) >= 0.0, key
     assert fft.get_measurement("first_trans") == 0.0  # fused into the kernels
+    assert fft.get_measurement("gbps") > 0.0 and fft.get_measurement("gflops") > 0.0
+    assert 0.0 < fft.get_measurement("roofline") < 2.0  # of the nominal DRAM bandwidth
     assert fft.get_measurement("no such key") == 0.0  # loop.cpp:192 default-inserts 0
     path = tmp_path / "plans" / "plan.txt"
     with pytest.raises(RuntimeError, match="Failed to open file"):
@@ -120,3 +122,27 @@ def test_cpp_shared_loop_driver(gpu_lib, cuda, build_mod, tmp_path):
     assert rows[1].split(";")[1:5] == ["64", "96", "estimate", "par"]
     plan = (tmp_path / "plans" / "plan_hpx_shared_loop.txt").read_text()
     assert "GPU r2c 1D plan:" in plan and "GPU c2c 1D plan:" in plan
+
+
+def test_loop_backward_and_precisions(gpu_lib, cuda):
+    """fft_2d_r2c_backward on the reference-style class (adjoint of an
+    impulse at DC is all ones), and the FP32 / split-BF16 variants."""
+    nx, ny = 1024, 64
+    nc = 2 * (ny // 2 + 1)
+    fft = gpu_lib.shared.loop()
+    fft.initialize(gpu_lib.util.vector_2d(nx, nc), "estimate")
+    g = gpu_lib.util.vector_2d(nx, nc)
+    g[0, 0] = 1.0  # G[0][0] = 1: L = Re X[0][0] = sum of the inputs
+    grad = fft.fft_2d_r2c_backward(g).data().reshape(nx, nc)
+    assert np.allclose(grad[:, :ny], 1.0, rtol=0, atol=1e-13) and not grad[:, ny:].any()
+    assert fft.get_measurement("total") > 0.0
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-1, 1, (nx, ny))
+    for prec, tol in (("f32", 2e-6), ("bf16x3", 2e-6)):
+        v = gpu_lib.util.vector_2d(nx, nc, dtype=np.float32)
+        v.data()[:, :ny] = x
+        f = gpu_lib.shared.loop()
+        f.initialize(v, "estimate", precision=prec)
+        out = f.fft_2d_r2c().data().reshape(nx, nc).astype(np.float64).view(np.complex128)
+        ref = np.fft.rfft2(x.astype(np.float32).astype(np.float64))
+        assert np.linalg.norm(out - ref) / np.linalg.norm(ref) <= tol, prec
