@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -34,6 +35,7 @@ sys.path.insert(0, os.path.join(REPO, "hpx-fft_gb300", "python"))
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 
 METRIC = "2D r2c FFT ms & HBM GB/s at 16384²: FP64 drop-in vs FP32/split-BF16 at rel-L2 err"
+NOMINAL_HBM_GBS = 7900.0  # GB300 HBM3e, nominal
 UNIT = "GB/s"
 
 
@@ -368,6 +370,8 @@ def run_ours(args):
             },
             "gpu_launches": (1 + steps) * args.steps,
             "kernels_ms": dict({k: 1e3 * v for k, v in kernels.items()}, count=stats["count"]),
+            "gflops": world * 2.5 * nx * ny * math.log2(nx * ny) / (ms * 1e-3) / 1e9,
+            "frac_of_nominal_hbm": value / NOMINAL_HBM_GBS,
             "roofline": {
                 "bound": "hbm",
                 "kernel": dominant,

@@ -85,6 +85,7 @@ struct hpxfft_plan_s {
     cudaEvent_t ev_copy[2] = {};  // before the host->device copy, after the device->host copy
     bool pending_copy = false;
     bool last_zero_copy = false;  // the last host-buffer transform read and wrote host memory directly
+    bool columns_only = false;    // the column pass alone (the first axis of a 3D transform)
     double peak_gbps = 0.0;       // nominal DRAM bandwidth of the device (memory clock x bus width)
     double sum_first = 0, sum_second = 0, sum_total = 0, sum_step_a = 0;
     long long nsum = 0;
@@ -574,6 +575,30 @@ static cudaError_t dispatch_forward(hpxfft_plan_s &p, const void *in, void *out,
     }
 }
 
+// The column pass alone, forward, in place (timed like a transform: the
+// row slot of the timing ring is empty).
+template <class A>
+static cudaError_t run_columns_only(hpxfft_plan_s &p, void *data)
+{
+    cudaError_t e;
+    cudaEvent_t *ev = next_slot(p);
+    if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
+    if ((e = run_columns<A>(p, data, -1, data)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(ev[2], p.stream)) != cudaSuccess) return e;
+    ++p.next;
+    return cudaSuccess;
+}
+
+static cudaError_t dispatch_columns_only(hpxfft_plan_s &p, void *data)
+{
+    switch (p.prec) {
+    case HPXFFT_PREC_F64: return run_columns_only<ArithFF>(p, data);
+    case HPXFFT_PREC_F64_NATIVE: return run_columns_only<ArithF64>(p, data);
+    default: return run_columns_only<ArithF32>(p, data);
+    }
+}
+
 static cudaError_t dispatch_inverse(hpxfft_plan_s &p, void *data, int adjoint)
 {
     switch (p.prec) {
@@ -681,8 +706,13 @@ const char *hpxfft_last_error(void) { return g_last_error.c_str(); }
 
 int hpxfft_plan_flag_valid(const char *plan_flag) { return valid_flag(plan_flag) ? 1 : 0; }
 
-int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batch, int precision,
-                       const char *plan_flag)
+}  // extern "C"
+
+// columns_only: a plan of the column pass alone (c2c along n_row of n_col/2
+// complex columns), the last axis of a 3D transform; no row plan, no row
+// twiddles, no float-float pair exchange.
+static int create_plan(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batch, int precision,
+                       const char *plan_flag, bool columns_only)
 {
     if (!out) return fail(HPXFFT_ERR_INVALID_ARG, "plan pointer is null");
     *out = nullptr;
@@ -706,7 +736,8 @@ int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
     p->flag = plan_flag;
     p->real_bytes = f32_storage(precision) ? 4 : 8;
     p->tw_elem = f32_storage(precision) ? 8 : 16;
-    if (!plan_rows(*p) || !plan_cols(*p)) {
+    p->columns_only = columns_only;
+    if ((!columns_only && !plan_rows(*p)) || !plan_cols(*p)) {
         delete p;
         return fail(HPXFFT_ERR_UNSUPPORTED_SIZE,
                     "sizes must have no prime factor above 13 and fit the per-cluster shared memory");
@@ -732,12 +763,12 @@ int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
             hpxfft_plan_destroy(p);
             return cuda_fail(e, "event");
         }
-    if (cudaMalloc(&p->tw_row, p->tw_elem * 2 * p->M) != cudaSuccess ||
+    if ((!columns_only && cudaMalloc(&p->tw_row, p->tw_elem * 2 * p->M) != cudaSuccess) ||
         cudaMalloc(&p->tw_col, p->tw_elem * p->nx) != cudaSuccess) {
         hpxfft_plan_destroy(p);
         return fail(HPXFFT_ERR_ALLOC, "twiddle tables");
     }
-    int rc = setup_fixed(*p, p->row, true, p->stream);
+    int rc = columns_only ? HPXFFT_OK : setup_fixed(*p, p->row, true, p->stream);
     if (rc == HPXFFT_OK) rc = setup_fixed(*p, p->col, false, p->stream);
     // column strategy: the two-kernel pass streams 512-byte row segments and
     // wins once the cluster kernel needs 8 or more CTAs per strip
@@ -772,7 +803,7 @@ int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
                 // tensor-core row, whose BF16 split costs more CUDA-core
                 // work than the radix-16 butterfly it replaces)
                 const char *rows_env = std::getenv("HPXFFT_TC_ROWS");
-                if (p->row.FL && TcRowLaunch::supports((int)p->M, p->row.log2W, p->row.C) &&
+                if (!columns_only && p->row.FL && TcRowLaunch::supports((int)p->M, p->row.log2W, p->row.C) &&
                     !(rows_env && !strcmp(rows_env, "0")))
                     p->tc_rows = true;
             }
@@ -793,7 +824,7 @@ int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
     // float-float pair exchange between the forward kernels (compiled step
     // shapes only); HPXFFT_FF_PAIRS=0 keeps doubles in between (tests, tuning)
     const char *pairs_env = std::getenv("HPXFFT_FF_PAIRS");
-    if (rc == HPXFFT_OK && precision == HPXFFT_PREC_F64 && p->col_two_step && p->colA.FL && p->colB.FL &&
+    if (rc == HPXFFT_OK && !columns_only && precision == HPXFFT_PREC_F64 && p->col_two_step && p->colA.FL && p->colB.FL &&
         p->colA.L <= kColStepMaxPairL && p->colB.L <= kColStepMaxPairL && !(pairs_env && !strcmp(pairs_env, "0"))) {
         if (cudaMalloc(&p->exp_rows, sizeof(int) * p->nx * p->batch) != cudaSuccess ||
             cudaMalloc(&p->exp_step_a, sizeof(int) * p->colA.shape.grid.x * p->batch) != cudaSuccess) {
@@ -808,7 +839,7 @@ int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
         hpxfft_plan_destroy(p);
         return fail(rc, msg);
     }
-    if ((e = gen_twiddles(precision, p->tw_row, (int)(2 * p->M), p->stream)) != cudaSuccess ||
+    if ((!columns_only && (e = gen_twiddles(precision, p->tw_row, (int)(2 * p->M), p->stream)) != cudaSuccess) ||
         (e = gen_twiddles(precision, p->tw_col, (int)p->nx, p->stream)) != cudaSuccess ||
         (e = cudaStreamSynchronize(p->stream)) != cudaSuccess) {
         hpxfft_plan_destroy(p);
@@ -831,6 +862,110 @@ int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
     p->meas["plan_flops"] = ny * f_r2c + nx * f_c2c;
     p->meas["plan_flops_actual"] = (nx * f_r2c + (double)p->dcy * f_c2c) * (double)batch;
     *out = p;
+    return HPXFFT_OK;
+}
+
+extern "C" {
+
+int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batch, int precision,
+                       const char *plan_flag)
+{
+    return create_plan(out, n_row, n_col, batch, precision, plan_flag, false);
+}
+
+// ------------------------------------------------------------------ 3D r2c
+// n0 x n1 x n2 reals, last axis padded to n_col = 2 (n2/2 + 1):  a batched
+// 2D r2c over the n0 slabs (rows along axis 2, columns along axis 1), then
+// the column pass along axis 0 over the n1 (n2/2 + 1) complex columns of
+// the slab-major layout (rows of n1 n_col reals).
+struct hpxfft_plan3d_s {
+    hpxfft_plan slabs = nullptr;
+    hpxfft_plan axis0 = nullptr;
+    size_t n0 = 0, n1 = 0, ncol = 0, batch = 1;
+};
+
+int hpxfft_plan3d_create(hpxfft_plan3d *out, size_t n0, size_t n1, size_t n_col, size_t batch, int precision,
+                         const char *plan_flag)
+{
+    if (!out) return fail(HPXFFT_ERR_INVALID_ARG, "plan pointer is null");
+    *out = nullptr;
+    if (n0 == 0 || n1 == 0 || batch == 0) return fail(HPXFFT_ERR_INVALID_ARG, "empty array");
+    if (n0 * batch > 65535) return fail(HPXFFT_ERR_UNSUPPORTED_SIZE, "n0 * batch must not exceed 65535");
+    if (n1 * n_col > (1u << 30)) return fail(HPXFFT_ERR_UNSUPPORTED_SIZE, "dimension too large");
+    hpxfft_plan3d_s *p = new (std::nothrow) hpxfft_plan3d_s();
+    if (!p) return fail(HPXFFT_ERR_ALLOC, "host allocation failed");
+    p->n0 = n0;
+    p->n1 = n1;
+    p->ncol = n_col;
+    p->batch = batch;
+    int rc = create_plan(&p->slabs, n1, n_col, n0 * batch, precision, plan_flag, false);
+    if (rc == HPXFFT_OK) rc = create_plan(&p->axis0, n0, n1 * n_col, batch, precision, plan_flag, true);
+    if (rc != HPXFFT_OK) {
+        std::string msg = g_last_error;
+        hpxfft_plan3d_destroy(p);
+        return fail(rc, msg);
+    }
+    p->axis0->stream = p->slabs->stream;  // one stream orders both passes
+    *out = p;
+    return HPXFFT_OK;
+}
+
+int hpxfft_plan3d_destroy(hpxfft_plan3d p)
+{
+    if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
+    if (p->axis0) {
+        p->axis0->stream = p->axis0->own_stream;
+        hpxfft_plan_destroy(p->axis0);
+    }
+    if (p->slabs) hpxfft_plan_destroy(p->slabs);
+    delete p;
+    return HPXFFT_OK;
+}
+
+int hpxfft_plan3d_set_stream(hpxfft_plan3d p, void *stream)
+{
+    if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
+    p->slabs->stream = (cudaStream_t)stream;
+    p->axis0->stream = (cudaStream_t)stream;
+    return HPXFFT_OK;
+}
+
+int hpxfft_plan3d_buffer_bytes(hpxfft_plan3d p, size_t *bytes)
+{
+    if (!p || !bytes) return fail(HPXFFT_ERR_INVALID_ARG, "null argument");
+    *bytes = p->n0 * p->n1 * p->ncol * p->slabs->real_bytes * p->batch;
+    return HPXFFT_OK;
+}
+
+int hpxfft_execute3d_r2c(hpxfft_plan3d p, void *d)
+{
+    if (!p) return fail(HPXFFT_ERR_STATE, "null plan");
+    if (!d) return fail(HPXFFT_ERR_INVALID_ARG, "null device buffer");
+    if ((uintptr_t)d & 15) return fail(HPXFFT_ERR_INVALID_ARG, "buffers must be 16-byte aligned");
+    cudaError_t e = dispatch_forward(*p->slabs, d, d);
+    if (e == cudaSuccess) e = dispatch_columns_only(*p->axis0, d);
+    if (e != cudaSuccess) return cuda_fail(e, "3D forward launch");
+    return HPXFFT_OK;
+}
+
+int hpxfft_plan3d_get_measurement(hpxfft_plan3d p, const char *name, double *value)
+{
+    if (!p || !name || !value) return fail(HPXFFT_ERR_INVALID_ARG, "null argument");
+    double a = 0, b = 0, c = 0;
+    int rc = hpxfft_get_measurement(p->slabs, "first_fftw", &a);
+    if (rc == HPXFFT_OK) rc = hpxfft_get_measurement(p->slabs, "second_fftw", &b);
+    if (rc == HPXFFT_OK) rc = hpxfft_get_measurement(p->axis0, "total", &c);
+    if (rc != HPXFFT_OK) return rc;
+    if (!strcmp(name, "total"))
+        *value = a + b + c;
+    else if (!strcmp(name, "first_fftw"))
+        *value = a;  // rows (axis 2)
+    else if (!strcmp(name, "second_fftw"))
+        *value = b;  // axis 1
+    else if (!strcmp(name, "third_fftw"))
+        *value = c;  // axis 0
+    else
+        return hpxfft_get_measurement(p->slabs, name, value);
     return HPXFFT_OK;
 }
 

@@ -59,6 +59,12 @@ SIGNATURES = {
     "hpxfft_batch_synchronize": (_ci, [_vp]),
     "hpxfft_plan_synchronize": (_ci, [_vp]),
     "hpxfft_execute_r2c_backward_host": (_ci, [_vp, _vp]),
+    "hpxfft_plan3d_create": (_ci, [ctypes.POINTER(_vp), _sz, _sz, _sz, _sz, _ci, _cs]),
+    "hpxfft_plan3d_destroy": (_ci, [_vp]),
+    "hpxfft_plan3d_set_stream": (_ci, [_vp, _vp]),
+    "hpxfft_plan3d_buffer_bytes": (_ci, [_vp, ctypes.POINTER(_sz)]),
+    "hpxfft_execute3d_r2c": (_ci, [_vp, _vp]),
+    "hpxfft_plan3d_get_measurement": (_ci, [_vp, _cs, ctypes.POINTER(ctypes.c_double)]),
     "hpxfft_batch_get_measurement": (_ci, [_vp, _cs, ctypes.POINTER(ctypes.c_double)]),
     "hpxfft_wisdom_export": (_ci, [_cs]),
     "hpxfft_wisdom_import": (_ci, [_cs]),

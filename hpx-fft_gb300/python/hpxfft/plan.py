@@ -150,3 +150,52 @@ class Plan:
 
 def plan_flag_valid(flag: str) -> bool:
     return bool(_capi.load().hpxfft_plan_flag_valid(flag.encode()))
+
+
+class Plan3D:
+    """A planned 3D r2c of `batch` arrays of n0 x n1 x n2 reals, the last axis
+    padded to n_col = 2*(n2/2+1); in place, output X[k0][k1][k2] (n_col/2
+    complex along the last axis), numpy.fft.rfftn orientation."""
+
+    def __init__(self, n0: int, n1: int, n_col: int, batch: int = 1, precision="f64", plan_flag: str = "estimate"):
+        lib = _capi.load()
+        self._lib = lib
+        self._h = ctypes.c_void_p()
+        _capi.check(lib.hpxfft_plan3d_create(ctypes.byref(self._h), n0, n1, n_col, batch, precision_code(precision),
+                                             plan_flag.encode()))
+        self.shape = (int(n0), int(n1), int(n_col))
+        self.batch = int(batch)
+        self.dtype = real_dtype(precision)
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        _capi.check(self._lib.hpxfft_plan3d_set_stream(self._h, ctypes.c_void_p(stream_handle or 0)))
+
+    def execute_device(self, ptr: int) -> None:
+        _capi.check(self._lib.hpxfft_execute3d_r2c(self._h, ctypes.c_void_p(ptr)))
+
+    def buffer_bytes(self) -> int:
+        n = ctypes.c_size_t()
+        _capi.check(self._lib.hpxfft_plan3d_buffer_bytes(self._h, ctypes.byref(n)))
+        return n.value
+
+    def measurement(self, name: str) -> float:
+        v = ctypes.c_double()
+        _capi.check(self._lib.hpxfft_plan3d_get_measurement(self._h, name.encode(), ctypes.byref(v)))
+        return v.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.hpxfft_plan3d_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -57,6 +57,7 @@ typedef enum {
 } hpxfft_precision;
 
 typedef struct hpxfft_plan_s *hpxfft_plan;
+typedef struct hpxfft_plan3d_s *hpxfft_plan3d;
 
 /* Plan a 2D r2c of `batch` equally sized arrays of n_row x n_col reals
  * (n_col = 2*(ny/2+1), so ny = n_col - 2).  plan_flag is one of
@@ -145,6 +146,22 @@ HPXFFT_API int hpxfft_write_plan(hpxfft_plan plan, const char *file_path);
 
 /* 1 if plan_flag is a valid plan flag string, else 0. */
 HPXFFT_API int hpxfft_plan_flag_valid(const char *plan_flag);
+
+/* 3D r2c of `batch` arrays of n0 x n1 x n2 reals, the last axis padded to
+ * n_col = 2*(n2/2+1) (the 2D layout with one more leading axis); in place,
+ * output X[k0][k1][k2], k2 <= n2/2, unnormalised (numpy.fft.rfftn).  A
+ * batched 2D r2c over the n0 slabs, then the column pass along axis 0.
+ * n0 * batch <= 65535.  No reference counterpart (the reference is 2D
+ * only; "multidimensional" in its title). */
+HPXFFT_API int hpxfft_plan3d_create(hpxfft_plan3d *plan, size_t n0, size_t n1, size_t n_col, size_t batch,
+                                    int precision, const char *plan_flag);
+HPXFFT_API int hpxfft_plan3d_destroy(hpxfft_plan3d plan);
+HPXFFT_API int hpxfft_plan3d_set_stream(hpxfft_plan3d plan, void *cuda_stream);
+HPXFFT_API int hpxfft_plan3d_buffer_bytes(hpxfft_plan3d plan, size_t *bytes);
+HPXFFT_API int hpxfft_execute3d_r2c(hpxfft_plan3d plan, void *device_values);
+/* "total", "first_fftw" (axis 2), "second_fftw" (axis 1), "third_fftw"
+ * (axis 0) of the last transform, seconds; other keys as the 2D plan. */
+HPXFFT_API int hpxfft_plan3d_get_measurement(hpxfft_plan3d plan, const char *name, double *value);
 
 /* Static description of a status code; message of the calling thread's
  * most recent failure. */
