@@ -746,6 +746,83 @@ __global__ void HPXFFT_BOUNDS(A, FL) row_c2r_kernel(RowArgs a)
     const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
     const cpx<T> *ptab = reinterpret_cast<const cpx<T> *>(a.ptab);
 
+    if constexpr (kFixed && C == 1 && !A::kScaled) {
+        // FP32: Hermitian pre-processing and the first pass in registers from
+        // global memory, the last pass straight to the real output rows
+        constexpr int NT = fixed_threads(FL, FW, EPT);
+        constexpr int R1 = fixed_radix(FL, 1, EPT), LR1 = FL / R1;
+        constexpr int NTASK = LR1 << FW, TPT = (NTASK + NT - 1) / NT;
+        const bool active = tid < NT;
+#pragma unroll
+        for (int t = 0; t < TPT; ++t) {
+            const int task = tid + t * NT;
+            if (active && (NTASK % NT == 0 || task < NTASK)) {
+                const int w = task & wmask, jj = task >> log2W, row = row0 + w;
+                cpx<T> v[R1];
+                constexpr int H = R1 > 8 ? 8 : R1;  // loads in flight per batch (register budget)
+#pragma unroll
+                for (int r0 = 0; r0 < R1; r0 += H) {
+                    float2 xa[H], xb[H];
+#pragma unroll
+                    for (int h = 0; h < H; ++h) {
+                        const int k = jj + (r0 + h) * LR1;
+                        xa[h] = xb[h] = make_float2(0.f, 0.f);
+                        if (row < a.nrows) {
+                            xa[h] = ld_stream(in + row * a.in_stride + 2 * (long long)k);
+                            xb[h] = ld_stream(in + row * a.in_stride + 2 * (long long)(M - k));
+                        }
+                    }
+#pragma unroll
+                    for (int h = 0; h < H; ++h) {
+                        const int k = jj + (r0 + h) * LR1;
+                        cpx<T> za{xa[h].x, xa[h].y}, zb{xb[h].x, xb[h].y};
+                        if (k == 0) {
+                            za.im = 0;
+                            zb.im = 0;
+                        } else if (a.adjoint) {
+                            za = chalf(za);
+                            zb = chalf(zb);
+                        }
+                        const cpx<T> zbc = cconj(zb);
+                        v[r0 + h] = (za + zbc) + mul_i<+1>(cmul(twid<+1>(tw, k), za - zbc));
+                    }
+                }
+                DFT<R1, +1, T>::run(v);
+#pragma unroll
+                for (int r = 0; r < R1; ++r) s[pidx(((jj * R1 + r) << log2W) + w)] = v[r];
+            }
+        }
+        __syncthreads();
+        constexpr int LSL = last_pass_ls(FL, EPT), RL = fixed_radix(FL, LSL, EPT), LRL = FL / RL;
+        FixedPassRange<T, FL, (1 << FW), NT, +1, EPT, R1, 0, LSL>::run(s, ptab);
+        constexpr int Off = pass_table_offset(FL, EPT, LSL);
+        constexpr int NTL = LRL << FW, TPTL = (NTL + NT - 1) / NT;
+#pragma unroll
+        for (int t = 0; t < TPTL; ++t) {
+            const int task = tid + t * NT;
+            if (active && (NTL % NT == 0 || task < NTL)) {
+                const int w = task & wmask, jj = task >> log2W, row = row0 + w;
+                const int k = jj % LSL;
+                cpx<T> v[RL];
+#pragma unroll
+                for (int r = 0; r < RL; ++r) v[r] = s[pidx(((jj + r * LRL) << log2W) + w)];
+#pragma unroll
+                for (int r = 1; r < RL; ++r) v[r] = cmul(v[r], twid<+1>(ptab + Off, (r - 1) * LSL + k));
+                DFT<RL, +1, T>::run(v);
+                if (row < a.nrows) {
+                    const int base = (jj - k) * RL + k;
+#pragma unroll
+                    for (int r = 0; r < RL; ++r)
+                        store_c<A>(out + row * a.out_stride + 2 * (long long)(base + r * LSL), v[r], 0);
+                    if (task < (1 << log2W)) {  // jj == 0: the row's two pad reals
+                        out[row * a.out_stride + 2 * (long long)M] = (S)0;
+                        out[row * a.out_stride + 2 * (long long)M + 1] = (S)0;
+                    }
+                }
+            }
+        }
+        return;
+    }
     int emax = 0;
     if constexpr (A::kScaled) {
         if (tid < 64) sE[tid] = 0;
