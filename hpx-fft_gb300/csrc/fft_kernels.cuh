@@ -929,6 +929,60 @@ __device__ __forceinline__ void col_body(const ColArgs &a, int strip, int bidx)
     const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
     const cpx<T> *ptab = reinterpret_cast<const cpx<T> *>(a.ptab);
 
+    if constexpr (kFixed && C == 1 && !A::kScaled) {
+        // FP32: first pass from global memory into registers, last pass back
+        // to it (in place is safe: every read of the strip precedes the CTA
+        // barrier after the first pass, strips of other CTAs are disjoint)
+        constexpr int NT = fixed_threads(FL, FW, EPT);
+        constexpr int R1 = fixed_radix(FL, 1, EPT), LR1 = FL / R1;
+        constexpr int NTASK = LR1 << FW, TPT = (NTASK + NT - 1) / NT;
+        const bool active = tid < NT;
+#pragma unroll
+        for (int t = 0; t < TPT; ++t) {
+            const int task = tid + t * NT;
+            if (active && (NTASK % NT == 0 || task < NTASK)) {
+                const int w = task & wmask, jj = task >> log2W, col = col0 + w;
+                float2 raw[R1];
+#pragma unroll
+                for (int r = 0; r < R1; ++r) {
+                    raw[r] = make_float2(0.f, 0.f);
+                    if (col < a.ncols) raw[r] = ld_stream(data + (long long)(jj + r * LR1) * a.row_stride + 2 * (long long)col);
+                }
+                cpx<T> v[R1];
+#pragma unroll
+                for (int r = 0; r < R1; ++r) v[r] = cpx<T>{raw[r].x, raw[r].y};
+                DFT<R1, DIR, T>::run(v);
+#pragma unroll
+                for (int r = 0; r < R1; ++r) s[pidx(((jj * R1 + r) << log2W) + w)] = v[r];
+            }
+        }
+        __syncthreads();
+        constexpr int LSL = last_pass_ls(FL, EPT), RL = fixed_radix(FL, LSL, EPT), LRL = FL / RL;
+        FixedPassRange<T, FL, (1 << FW), NT, DIR, EPT, R1, 0, LSL>::run(s, ptab);
+        constexpr int Off = pass_table_offset(FL, EPT, LSL);
+        constexpr int NTL = LRL << FW, TPTL = (NTL + NT - 1) / NT;
+#pragma unroll
+        for (int t = 0; t < TPTL; ++t) {
+            const int task = tid + t * NT;
+            if (active && (NTL % NT == 0 || task < NTL)) {
+                const int w = task & wmask, jj = task >> log2W, col = col0 + w;
+                const int k = jj % LSL;
+                cpx<T> v[RL];
+#pragma unroll
+                for (int r = 0; r < RL; ++r) v[r] = s[pidx(((jj + r * LRL) << log2W) + w)];
+#pragma unroll
+                for (int r = 1; r < RL; ++r) v[r] = cmul(v[r], twid<DIR>(ptab + Off, (r - 1) * LSL + k));
+                DFT<RL, DIR, T>::run(v);
+                if (col < a.ncols) {
+                    const int base = (jj - k) * RL + k;
+#pragma unroll
+                    for (int r = 0; r < RL; ++r)
+                        store_c<A>(data + (long long)(base + r * LSL) * a.row_stride + 2 * (long long)col, v[r], 0);
+                }
+            }
+        }
+        return;
+    }
     using V2 = typename std::conditional<sizeof(S) == 8, double2, float2>::type;
     auto ld_col = [&](int t) {
         const int w = t & wmask, m = t >> log2W, col = col0 + w;
