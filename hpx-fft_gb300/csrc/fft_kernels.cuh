@@ -511,6 +511,83 @@ __device__ __forceinline__ void row_r2c_split(const cpx<typename A::T> *s, const
     }
 }
 
+// Last pass of a compile-time row chain fused with the packed-real split.
+// Task jj of the last pass (Ls = LSL, radix RL) yields Z[jj + r LSL]; task
+// LSL - jj yields their split partners Z[M - k], so a thread that runs both
+// holds every (k, M - k) pair in registers and writes X[k], X[M - k] itself.
+// Pair tasks: jj in [0, LSL/2] per row (jj = 0 and jj = LSL/2 pair with
+// themselves).
+template <class A, int FL, int FW, int NT>
+__device__ __forceinline__ void row_last_pass_split(const cpx<typename A::T> *s,
+                                                    const cpx<typename A::T> *__restrict__ ptab, const RowArgs &a,
+                                                    int row0, const cpx<typename A::T> *__restrict__ tw,
+                                                    typename A::S *out, int bidx, const int *sEc)
+{
+    using T = typename A::T;
+    using S = typename A::S;
+    constexpr int EPT = A::kEPTFixed, W = 1 << FW;
+    constexpr int LSL = last_pass_ls(FL, EPT), RL = fixed_radix(FL, LSL, EPT), LRL = FL / RL;
+    constexpr int Off = pass_table_offset(FL, EPT, LSL);
+    constexpr int NPAIR = (LSL / 2 + 1) * W, TPT = (NPAIR + NT - 1) / NT;
+    constexpr int M = FL;
+    const cpx<T> *tp = ptab + Off;
+    const int tid = threadIdx.x;
+    if (tid >= NT) return;
+    auto last_task = [&](int jj, int w, cpx<T> (&v)[RL]) {
+#pragma unroll
+        for (int r = 0; r < RL; ++r) v[r] = s[pidx(((jj + r * LRL) << FW) + w)];
+#pragma unroll
+        for (int r = 1; r < RL; ++r) v[r] = cmul(v[r], twid<-1>(tp, (r - 1) * LSL + jj));
+        DFT<RL, -1, T>::run(v);
+    };
+#pragma unroll
+    for (int t = 0; t < TPT; ++t) {
+        const int task = tid + t * NT;
+        if (!(NPAIR % NT == 0 || task < NPAIR)) continue;
+        const int w = task % W, jj = task / W, row = row0 + w;
+        if (row >= a.nrows) continue;
+        const int jj2 = (LSL - jj) % LSL;
+        cpx<T> va[RL], vb[RL];
+        last_task(jj, w, va);
+        if (jj2 != jj) last_task(jj2, w, vb);
+        const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
+        S *orow = out + (long long)row * a.out_stride;
+        auto emit = [&](int k, cpx<T> zk, cpx<T> zp) {  // k <= M/2, zp = Z[M - k]
+            const cpx<T> zb = cconj(zp);
+            const cpx<T> e = chalf(zk + zb), o = chalf(zk - zb);
+            const cpx<T> tk = cmul(tw[k], o);
+            if (A::kScaled && a.pairs_out) {
+                store_pair<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk));
+                if (M - k != k) store_pair<A>(orow + 2 * (long long)(M - k), cconj(e + mul_i<+1>(tk)));
+                if (k == 0) a.exp_out[(long long)bidx * a.nrows + row] = block_exp(sEc[w]);
+            } else {
+                store_c<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk), E);
+                if (M - k != k) store_c<A>(orow + 2 * (long long)(M - k), cconj(e + mul_i<+1>(tk)), E);
+            }
+        };
+#pragma unroll
+        for (int r = 0; r < RL; ++r) {
+            const int k = jj + r * LSL;  // an output of task jj
+            if (jj2 != jj) {
+                // partner M - k = jj2 + (RL - 1 - r) LSL, an output of task jj2
+                const int kp = M - k;
+                if (k <= kp)
+                    emit(k, va[r], vb[RL - 1 - r]);
+                else
+                    emit(kp, vb[RL - 1 - r], va[r]);
+            } else if (jj == 0) {
+                // k = r LSL pairs with (RL - r) LSL in the same task (r = 0: k = 0 with itself)
+                const int rp = (RL - r) % RL;
+                if (r <= rp) emit(k, va[r], va[rp]);
+            } else {
+                // jj = LSL / 2: k pairs with LSL/2 + (RL - 1 - r) LSL
+                const int rp = RL - 1 - r;
+                if (r <= rp) emit(k, va[r], va[rp]);
+            }
+        }
+    }
+}
+
 template <class A, int C, int FL, int FW>
 __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bidx)
 {
@@ -590,6 +667,15 @@ __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bi
             }
         }
         __syncthreads();
+        constexpr int LSL = last_pass_ls(FL, EPT), RL = fixed_radix(FL, LSL, EPT);
+        // FP32: the last pass fused with the packed-real split (16384^2 row
+        // 0.61 -> 0.53 ms); float-float measured slower that way (2.84 ->
+        // 2.94 ms, the 8192-pair CTA runs out of registers)
+        if constexpr (LSL > 1 && !A::kScaled && RL <= 8) {
+            FixedPassRange<T, FL, (1 << FW), NT, -1, EPT, R1, 0, LSL>::run(s, ptab);
+            row_last_pass_split<A, FL, FW, NT>(s, ptab, a, row0, tw, out, bidx, sEc);
+            return;
+        }
         FixedPassRange<T, FL, (1 << FW), NT, -1, EPT, R1, 0, FL>::run(s, ptab);
     } else if constexpr (A::kScaled) {
         if (tid < 64) sE[tid] = 0;

@@ -198,3 +198,16 @@ def test_unsupported_factor_is_rejected(gpu_lib, cuda):
         with pytest.raises(gpu_lib.HpxFftError) as e:
             gpu_lib.Plan(n_row, n_col, 1, "f64", "estimate")
         assert e.value.status == gpu_lib._capi.HPXFFT_ERR_UNSUPPORTED_SIZE
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_every_compiled_row_shape(gpu_lib, cuda, oracle_lib, prec):
+    """Row lengths M = 128 .. 8192 (the compiled row chains, with the last
+    pass fused into the packed-real split where its radix allows), 39 rows so
+    packed row groups are ragged."""
+    rng = np.random.default_rng(39)
+    for ny in (256, 512, 1024, 2048, 4096, 8192, 16384):
+        x = rng.uniform(-1, 1, (39, ny))
+        got = forward(gpu_lib, cuda, x.astype(np.float32) if prec == "f32" else x, prec)
+        ref = oracle_fwd(oracle_lib, x.astype(np.float32).astype(np.float64) if prec == "f32" else x)
+        assert rel_l2(got, ref) <= TOL[prec], (prec, ny)
