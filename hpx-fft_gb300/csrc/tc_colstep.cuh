@@ -277,8 +277,14 @@ __global__ void __launch_bounds__(FL * (1 << FW) / 16, 1024 / (FL * (1 << FW) / 
     tc_teardown<NV>(&s_tmem);
     if (!ok) return;
 
-    FixedPassRange<float, FL, W, NV, -1, 16, 16, 0, FL>::run(s, ptab);
-    row_r2c_split<ArithF32>(s, a, row0, FW, tw, out, bidx, nullptr, tid, NV);
+    constexpr int LSL = last_pass_ls(FL, 16);
+    if constexpr (fixed_radix(FL, LSL, 16) <= 8) {  // last pass fused with the packed-real split
+        FixedPassRange<float, FL, W, NV, -1, 16, 16, 0, LSL>::run(s, ptab);
+        row_last_pass_split<ArithF32, FL, FW, NV>(s, ptab, a, row0, tw, out, bidx, nullptr);
+    } else {
+        FixedPassRange<float, FL, W, NV, -1, 16, 16, 0, FL>::run(s, ptab);
+        row_r2c_split<ArithF32>(s, a, row0, FW, tw, out, bidx, nullptr, tid, NV);
+    }
 }
 
 // The three BF16 splits of the real DFT-16 matrix B (K-major: row n of the
