@@ -176,6 +176,20 @@ def dist_env():
     return rank, world, local
 
 
+def replica_max_ms(ms: float, world: int) -> float:
+    """The slowest replica's step time (max over ranks): with N independent
+    replicas the whole-job rate is N x one replica's bytes over this time."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -284,10 +298,7 @@ def run_ours(args):
         barrier()
     ms = ev0.elapsed_time(ev1) / args.steps
     stats = plan.timing_stats()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replica_max_ms(ms, world)
     B = algorithmic_bytes(nx, ny, real_bytes)
     value = world * B / (ms * 1e-3) / 1e9
 
