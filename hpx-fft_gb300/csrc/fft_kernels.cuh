@@ -1331,10 +1331,11 @@ __device__ __forceinline__ void colstep_last_pass_global(const cpx<typename A::T
 // pair input (the block's scale comes from the producers' exponents, so no
 // data-dependent reduction has to precede the first pass); the launcher
 // uses it for FP32.
+// Body of block (bx, by) of the grid: group bx / strips, strip bx % strips,
+// batch item by.  Threads past the shape's own count idle (the persistent
+// batch kernel runs it in larger CTAs).
 template <class A, int DIR, int FL, int FW>
-__global__ void __launch_bounds__(fixed_threads(FL, FW, A::kEPTFixed),
-                                  fixed_threads(FL, FW, A::kEPTFixed) <= kFixedThreadsMax ? kFixedMinBlocks : 1)
-    colstep_direct_kernel(ColStepArgs a)
+__device__ __forceinline__ void colstep_direct_body(const ColStepArgs &a, int bx, int by, int gx)
 {
     using T = typename A::T;
     using S = typename A::S;
@@ -1347,9 +1348,9 @@ __global__ void __launch_bounds__(fixed_threads(FL, FW, A::kEPTFixed),
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cpx<T> *s = reinterpret_cast<cpx<T> *>(smem_raw);
     const int tid = threadIdx.x;
-    const int g = blockIdx.x / a.strips, col0 = (blockIdx.x % a.strips) * W;
-    const S *in = reinterpret_cast<const S *>(a.in) + (long long)blockIdx.y * a.in_bstride;
-    S *out = reinterpret_cast<S *>(a.out) + (long long)blockIdx.y * a.out_bstride;
+    const int g = bx / a.strips, col0 = (bx % a.strips) * W;
+    const S *in = reinterpret_cast<const S *>(a.in) + (long long)by * a.in_bstride;
+    S *out = reinterpret_cast<S *>(a.out) + (long long)by * a.out_bstride;
     const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
     const cpx<T> *ptab = reinterpret_cast<const cpx<T> *>(a.ptab);
     const long long in_row0 = (long long)g * a.in_gmul, out_row0 = (long long)g * a.out_gmul;
@@ -1361,7 +1362,7 @@ __global__ void __launch_bounds__(fixed_threads(FL, FW, A::kEPTFixed),
         __shared__ float sFac[kColStepMaxPairL];
         if (tid == 0) sEm = kExpNone;
         __syncthreads();
-        const int *ein = a.exp_in + (long long)blockIdx.y * a.exp_in_bstride;
+        const int *ein = a.exp_in + (long long)by * a.exp_in_bstride;
         for (int m = tid; m < FL; m += NT) {
             const int r = (int)(in_row0 + (long long)a.in_step * m);
             const int e = ein[(r % a.exp_rmod) * a.exp_rmul + (col0 >> a.exp_cshift)];
@@ -1381,7 +1382,7 @@ __global__ void __launch_bounds__(fixed_threads(FL, FW, A::kEPTFixed),
 #pragma unroll
         for (int t = 0; t < TPT; ++t) {
             const int task = tid + t * NT;
-            if (NTASK % NT == 0 || task < NTASK) {
+            if (tid < NT && (NTASK % NT == 0 || task < NTASK)) {
                 const int w = task % W, jj = task / W, col = col0 + w;
                 const bool live = col < a.ncols;
                 cpx<T> v[R1];
@@ -1416,9 +1417,17 @@ __global__ void __launch_bounds__(fixed_threads(FL, FW, A::kEPTFixed),
 
     // last pass: outputs k = base + r LSL go straight to their rows
     const bool pairs_out = A::kScaled && a.pairs_out;
-    if (pairs_out && tid == 0) a.exp_out[blockIdx.x + (long long)gridDim.x * blockIdx.y] = Eblk;
+    if (pairs_out && tid == 0) a.exp_out[bx + (long long)gx * by] = Eblk;
     colstep_last_pass_global<A, DIR, FL, W, NT>(s, ptab, a, g, col0, out, out_row0, Eblk == kExpNone ? 0 : Eblk,
                                                 pairs_out);
+}
+
+template <class A, int DIR, int FL, int FW>
+__global__ void __launch_bounds__(fixed_threads(FL, FW, A::kEPTFixed),
+                                  fixed_threads(FL, FW, A::kEPTFixed) <= kFixedThreadsMax ? kFixedMinBlocks : 1)
+    colstep_direct_kernel(ColStepArgs a)
+{
+    colstep_direct_body<A, DIR, FL, FW>(a, blockIdx.x, blockIdx.y, gridDim.x);
 }
 
 // --------------------------------------------------------- twiddle tables
