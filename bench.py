@@ -7,7 +7,9 @@ value = algorithmic HBM bytes per step (4*S, S = nx*(ny/2+1)*16 B: the row
 pass reads and writes S, the column pass reads and writes S) / time.
 
 e2e = the same metric through the C ABI with host buffers
-(hpxfft_execute_r2c_host: pinned host array -> device -> transform -> host).
+(hpxfft_execute_r2c_host on a page-locked host array: the row kernel reads
+it and the last column step writes it over the host link, timed from the
+first byte read to the last byte written).
 
 --impl reference times the reference's algorithm on the host cores: the FP64
 C restatement of hpxfft::shared::loop (oracle/), because the reference itself

@@ -2,10 +2,11 @@
 //
 // The reference (core/src/shared/loop.cpp:56-113) runs four phases over host
 // memory: row r2c (FFTW), transpose, column c2c (FFTW), transpose back.  Here
-// the two transposes disappear: the column kernel works on strips of W
+// the two transposes disappear: the column kernels work on strips of W
 // adjacent ky columns directly in the [kx][ky] layout, so the whole 2D
 // transform is two HBM passes (row pass: read S, write S; column pass: read S,
-// write S) over the caller's padded in-place buffer.
+// write S) over the caller's padded in-place buffer, or three when long
+// columns take the two-kernel four-step split through a scratch array.
 //
 // One 1D transform of length N is held in shared memory.  When it does not
 // fit one CTA it is split over a thread-block cluster of C CTAs: CTA c owns

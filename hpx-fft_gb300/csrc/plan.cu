@@ -4,8 +4,10 @@
 // (core/src/shared/loop.cpp:158-189): the dimensions derived from the padded
 // buffer (dim_c_x = n_row, dim_c_y = n_col/2, dim_r_y = 2*dim_c_y - 2), one
 // row plan and one column plan.  Instead of FFTW plans it holds the launch
-// shapes of the two kernels, their radix sequences and FP64-generated
-// twiddle tables in HBM.
+// shapes of the row kernel and of the one or two column kernels, their radix
+// sequences and FP64-generated twiddle tables in HBM.  Also here: the
+// split-BF16 tensor-core stages, the host-buffer entry points (zero-copy on
+// page-locked memory), the 3D plans and the allocation-free entry point.
 #include <cuda_runtime.h>
 
 #include <chrono>

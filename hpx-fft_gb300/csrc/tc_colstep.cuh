@@ -1,4 +1,6 @@
-// Split-BF16 tensor-core column step (precision HPXFFT_PREC_BF16X3).
+// Split-BF16 tensor-core column step and row r2c (precision
+// HPXFFT_PREC_BF16X3).  The row kernel (bottom of this file) runs the same
+// tensor-core stage on the first pass of its rows.
 //
 // Same contract as colstep_kernel (one step of the four-step column FFT,
 // nx = N1 * N2), for DFT lengths L = 16 * L2, L2 in {2, 4, 8, 16}.  The first
