@@ -447,14 +447,18 @@ def profiled_traffic(prec, nx, ny, label):
         return None
     name = label.split(" ")[0]
     step = {"(A)": "(step A)", "(B)": "(step B)"}.get(label.split(" ")[-1]) if " " in label else None
+    col = None
     for line in open(path):
         cells = [c.strip() for c in line.strip().strip("|").split("|")]
-        if len(cells) < 8 or not cells[0].startswith("`" + name):
+        if col is None:
+            col = next((i for i, c in enumerate(cells) if c.startswith("traffic per")), None)
+            continue
+        if len(cells) <= col or not cells[0].startswith("`" + name):
             continue
         if step and step not in cells[0]:
             continue
         try:
-            return float(cells[6])
+            return float(cells[col])
         except ValueError:
             return None
     return None

@@ -63,3 +63,15 @@ def test_reference_arm_other_ranks_exit_silently():
                         "--warmup", "1"], env=env, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert r.stdout.strip() == ""
+
+
+def test_headline_kernels_have_profiled_traffic():
+    """bench.py's roofline.traffic comes from the committed ncu summary: every
+    kernel the FP64 16384^2 line can name as dominant must be found there,
+    at a plausible fraction of the algorithmic bytes per launch (2 S)."""
+    bench = _bench()
+    alg = 2 * 16384 * 16386 * 16
+    for label in ("row_r2c_kernel", "colstep_kernel (A)", "colstep_kernel (B)"):
+        t = bench.profiled_traffic("f64", 16384, 16384, label)
+        assert t is not None and 0.8 * alg <= t <= 1.5 * alg, (label, t)
+    assert bench.profiled_traffic("f32", 16384, 16384, "row_r2c_kernel") is None
