@@ -70,7 +70,7 @@ def test_headline_kernels_have_profiled_traffic():
     kernel the FP64 16384^2 line can name as dominant must be found there,
     at a plausible fraction of the algorithmic bytes per launch (2 S)."""
     bench = _bench()
-    alg = 2 * 16384 * 16386 * 16
+    alg = 2 * 16384 * 8193 * 16  # read + write of S = nx (ny/2+1) complex doubles
     for label in ("row_r2c_kernel", "colstep_kernel (A)", "colstep_kernel (B)"):
         t = bench.profiled_traffic("f64", 16384, 16384, label)
         assert t is not None and 0.8 * alg <= t <= 1.5 * alg, (label, t)
