@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP32 / batch / backward sections")
+    ap.add_argument("--batch-only", action="store_true", help="only the uneven FP32 batch (profiling)")
+    ap.add_argument("--batch-count", type=int, default=1024)
+    ap.add_argument("--batch-flag", default="measure", choices=["estimate", "measure"])
     args = ap.parse_args()
     args.nx = args.nx or args.n
     args.ny = args.ny or args.n
@@ -464,6 +467,38 @@ def profiled_traffic(prec, nx, ny, label):
     return None
 
 
+def batch_workload(torch, hpxfft, stream, count, flag, steps, warm, peak):
+    """`count` FP32 instances, nx and ny drawn independently from the
+    2^k, 3*2^k, 5*2^k sizes between 256 and 4096 (seeded), uniform[-1,1)
+    per-instance data, one persistent graph-replayed launch per step."""
+    sizes = [256, 384, 512, 640, 768, 1024, 1536, 2048, 2560, 3072, 4096]
+    rng = np.random.default_rng(1024)
+    shapes = [(int(rng.choice(sizes)), int(rng.choice(sizes))) for _ in range(count)]
+    with hpxfft.Batch([a for a, _ in shapes], [2 * (b // 2 + 1) for _, b in shapes], "f32", flag) as bt:
+        arena = torch.zeros(bt.arena_bytes // 4, dtype=torch.float32, device="cuda")
+        src = torch.empty_like(arena)
+        for i, ((r, c), off) in enumerate(zip(shapes, bt.offsets)):
+            g = torch.Generator(device="cuda")
+            g.manual_seed(7919 * i + 1)
+            w = 2 * (c // 2 + 1)
+            src[off // 4: off // 4 + r * w].view(r, w)[:, :c] = torch.rand((r, c), generator=g, device="cuda") * 2 - 1
+        arena.copy_(src)
+        del src
+        bt.set_stream(stream.cuda_stream)
+        ms = _time_steps(torch, stream, lambda: bt.execute(arena.data_ptr()), steps, warm)
+        bt.synchronize()
+        Bb = bt.measurement("algorithmic_bytes")
+        res = {"ms": ms, "value": Bb / (ms * 1e-3) / 1e9, "unit": "GB/s",
+               "frac_of_measured_hbm": Bb / (ms * 1e-3) / 1e9 / peak,
+               "instances": count, "items": bt.measurement("items"),
+               "tuned": {"flag": flag, "lag": bt.measurement("lag"), "ctas_per_sm": bt.measurement("ctas_per_sm"),
+                         "plan_s": bt.measurement("plan")},
+               "launches_per_step": 1, "cuda_graph": True,
+               "note": "in place, so steps after the first transform the previous output"}
+    del arena
+    return res
+
+
 def extras(torch, hpxfft, args, x64, oracle_ref, peak):
     """The other workloads of this path, measured in the same run:
     FP32 at the same size (precision), 1024 uneven FP32 transforms in one
@@ -500,32 +535,9 @@ def extras(torch, hpxfft, args, x64, oracle_ref, peak):
             out[f"precision_{prec}"] = sec
     del x32, y32
 
-    # batching: 1024 uneven FP32 instances
-    sizes = [256, 384, 512, 640, 768, 1024, 1536, 2048, 2560, 3072, 4096]
-    rng = np.random.default_rng(1024)
-    shapes = [(int(rng.choice(sizes)), int(rng.choice(sizes))) for _ in range(1024)]
-    # "measure": the plan step times queue orders once and caches the winner
-    with hpxfft.Batch([a for a, _ in shapes], [2 * (b // 2 + 1) for _, b in shapes], "f32", "measure") as bt:
-        arena = torch.zeros(bt.arena_bytes // 4, dtype=torch.float32, device="cuda")
-        src = torch.empty_like(arena)
-        for i, ((r, c), off) in enumerate(zip(shapes, bt.offsets)):
-            g = torch.Generator(device="cuda")
-            g.manual_seed(7919 * i + 1)
-            w = 2 * (c // 2 + 1)
-            src[off // 4: off // 4 + r * w].view(r, w)[:, :c] = torch.rand((r, c), generator=g, device="cuda") * 2 - 1
-        arena.copy_(src)
-        bt.set_stream(stream.cuda_stream)
-        ms = _time_steps(torch, stream, lambda: bt.execute(arena.data_ptr()), steps, warm)
-        bt.synchronize()
-        Bb = bt.measurement("algorithmic_bytes")
-        out["batch_1024_uneven_f32"] = {"ms": ms, "value": Bb / (ms * 1e-3) / 1e9, "unit": "GB/s",
-                                        "frac_of_measured_hbm": Bb / (ms * 1e-3) / 1e9 / peak,
-                                        "instances": 1024, "items": bt.measurement("items"),
-                                        "tuned": {"lag": bt.measurement("lag"), "ctas_per_sm": bt.measurement("ctas_per_sm"),
-                                                  "plan_s": bt.measurement("plan")},
-                                        "launches_per_step": 1, "cuda_graph": True,
-                                        "note": "in place, so steps after the first transform the previous output"}
-    del arena, src
+    # batching: 1024 uneven FP32 instances; "measure": the plan step times
+    # queue orders once and caches the winner
+    out["batch_1024_uneven_f32"] = batch_workload(torch, hpxfft, stream, 1024, "measure", steps, warm, peak)
 
     # differentiation: adjoint of the r2c on 64 FP32 2048^2 arrays
     nb, n = 64, 2048
@@ -542,10 +554,34 @@ def extras(torch, hpxfft, args, x64, oracle_ref, peak):
     return out
 
 
+def run_batch_only(args):
+    """The uneven FP32 batch alone, one JSON line (profiling the batch kernel
+    on fewer instances: --batch-count, --batch-flag estimate)."""
+    import importlib.util
+
+    import torch
+
+    torch.cuda.set_device(0)
+    spec = importlib.util.spec_from_file_location("hpxfft_build", os.path.join(REPO, "hpx-fft_gb300", "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    b.build_all()
+    import hpxfft
+
+    peak, _ = measured_peak_hbm()
+    res = batch_workload(torch, hpxfft, torch.cuda.current_stream(), args.batch_count, args.batch_flag,
+                         args.steps, max(3, args.warmup), peak)
+    res["workload"] = f"batch_{args.batch_count}_uneven_f32"
+    print(json.dumps(res), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.batch_only:
+        return run_batch_only(args)
     return run_ours(args)
 
 
