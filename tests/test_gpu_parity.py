@@ -158,6 +158,26 @@ def test_linearity_and_parseval(gpu_lib, cuda):
     assert abs(energy - np.sum(a * a)) <= 1e-12 * np.sum(a * a)
 
 
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_shift_theorem_and_exact_sinusoid_peaks(gpu_lib, cuda, prec):
+    """Oracle-free checks, the same helpers and shapes that
+    test_oracle.py::test_spectral_properties pins on the oracle: a circular
+    shift multiplies each bin by its exact phase, and integer-frequency
+    sinusoids give their exact sparse half spectrum."""
+    import spectral_properties as sp
+
+    tol = 1e-12 if prec == "f64" else 2e-6
+
+    def fwd(x):
+        return forward(gpu_lib, cuda, x, prec)
+
+    for nx, ny in ((77, 130), (96, 160), (256, 512), (2048, 4096)):
+        a = np.random.default_rng(nx * 7 + ny).uniform(-1, 1, (nx, ny))
+        assert sp.shift_error(fwd, a, nx // 3 + 1, -(ny // 5) - 1) <= tol, (nx, ny)
+        x, X = sp.pure_sinusoids(nx, ny, 4, nx + ny)
+        assert sp.rel_l2(fwd(x), X) <= tol, (nx, ny)
+
+
 def test_batch_of_equal_transforms(gpu_lib, cuda, oracle_lib):
     rng = np.random.default_rng(44)
     xs = rng.uniform(-1, 1, (5, 96, 80))

@@ -109,3 +109,63 @@ def test_rejects_bad_layout(oracle_lib):
         oracle_lib.fft_2d_r2c(np.zeros((4, 5)))
     with pytest.raises(ValueError):
         oracle_lib.fft_2d_r2c(np.zeros((4, 6), dtype=np.float32))
+
+
+PROPERTY_SHAPES = [(77, 130), (96, 160), (256, 512), (2048, 4096)]
+
+
+def oracle_forward(oracle_lib):
+    def fwd(x):
+        p = oracle_lib.padded(np.asarray(x, dtype=np.float64))
+        oracle_lib.fft_2d_r2c(p, nthreads=8)
+        return oracle_lib.spectrum(p)
+
+    return fwd
+
+
+@pytest.mark.parametrize("nx,ny", PROPERTY_SHAPES)
+def test_spectral_properties(oracle_lib, nx, ny):
+    """Linearity, Parseval, the shift theorem and exact sinusoid peaks: the
+    same checks the GPU parity suite runs on the CUDA path."""
+    import spectral_properties as sp
+
+    fwd = oracle_forward(oracle_lib)
+    rng = np.random.default_rng(nx * 7 + ny)
+    a, b = rng.uniform(-1, 1, (nx, ny)), rng.uniform(-1, 1, (nx, ny))
+    assert sp.linearity_error(fwd, a, b) <= 1e-14
+    assert sp.parseval_error(fwd, a) <= 1e-13
+    assert sp.shift_error(fwd, a, nx // 3 + 1, -(ny // 5) - 1) <= 1e-14
+    x, X = sp.pure_sinusoids(nx, ny, 4, nx + ny)
+    assert sp.rel_l2(fwd(x), X) <= 1e-14
+
+
+def test_spectral_properties_catch_planted_mistakes(oracle_lib):
+    """Each check fails on a transform with the mistake it is meant to see,
+    planted in the oracle's output: the wrong sign (conjugated spectrum), a
+    dropped bin and a stray scale."""
+    import spectral_properties as sp
+
+    fwd = oracle_forward(oracle_lib)
+    nx, ny = 96, 160
+    rng = np.random.default_rng(3)
+    a, b = rng.uniform(-1, 1, (nx, ny)), rng.uniform(-1, 1, (nx, ny))
+    x, X = sp.pure_sinusoids(nx, ny, 4, 11)
+
+    def conj(v):
+        return np.conj(fwd(v))
+
+    assert sp.shift_error(conj, a, 5, 7) > 0.1
+    assert sp.rel_l2(conj(x), X) > 0.1
+
+    def scaled(v):
+        return 1.001 * fwd(v)
+
+    assert sp.parseval_error(scaled, a) > 1e-3
+
+    def drops_bin(v):
+        out = fwd(v)
+        if np.abs(v).max() > 1.5:  # only the combined input
+            out[3, 4] = 0
+        return out
+
+    assert sp.linearity_error(drops_bin, a, b) > 1e-4
