@@ -168,6 +168,8 @@ class Plan3D:
         self.dtype = real_dtype(precision)
 
     def set_stream(self, stream_handle: int | None) -> None:
+        """Run both passes on a cudaStream_t handle; None or 0 = the legacy
+        default stream (a 3D plan starts on a stream of its own)."""
         _capi.check(self._lib.hpxfft_plan3d_set_stream(self._h, ctypes.c_void_p(stream_handle or 0)))
 
     def execute_device(self, ptr: int) -> None:

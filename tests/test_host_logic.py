@@ -57,6 +57,35 @@ def test_plan_argument_errors_before_any_device_call(gpu_lib):
     assert lib.hpxfft_execute_r2c(None, None) == gpu_lib._capi.HPXFFT_ERR_STATE
 
 
+def test_plan3d_argument_errors_before_any_device_call(gpu_lib):
+    capi = gpu_lib._capi
+    with pytest.raises(gpu_lib.HpxFftInvalidArgument, match="plan flag"):
+        gpu_lib.Plan3D(4, 4, 6, 1, "f64", "wisdom")
+    with pytest.raises(gpu_lib.HpxFftError) as e:
+        gpu_lib.Plan3D(4, 4, 5, 1, "f64", "estimate")  # odd n_col
+    assert e.value.status == capi.HPXFFT_ERR_UNSUPPORTED_SIZE
+    with pytest.raises(gpu_lib.HpxFftError) as e:
+        gpu_lib.Plan3D(256, 4, 6, 256, "f64", "estimate")  # n0 * batch > 65535
+    assert e.value.status == capi.HPXFFT_ERR_UNSUPPORTED_SIZE
+    for dims in ((0, 4, 6, 1), (4, 0, 6, 1), (4, 4, 6, 0)):
+        with pytest.raises(gpu_lib.HpxFftInvalidArgument):
+            gpu_lib.Plan3D(*dims, "f64", "estimate")
+    with pytest.raises(gpu_lib.HpxFftInvalidArgument):
+        gpu_lib.Plan3D(4, 4, 6, 1, "f16", "estimate")
+    lib = capi.load()
+    h = ctypes.c_void_p()
+    v = ctypes.c_double()
+    n = ctypes.c_size_t()
+    assert lib.hpxfft_plan3d_create(None, 4, 4, 6, 1, 0, b"estimate") == capi.HPXFFT_ERR_INVALID_ARG
+    assert lib.hpxfft_plan3d_create(ctypes.byref(h), 4, 4, 6, 1, 0, b"wisdom") == capi.HPXFFT_ERR_INVALID_ARG
+    assert h.value is None  # a failed create leaves the handle null
+    assert lib.hpxfft_plan3d_destroy(None) == capi.HPXFFT_ERR_STATE
+    assert lib.hpxfft_plan3d_set_stream(None, None) == capi.HPXFFT_ERR_STATE
+    assert lib.hpxfft_execute3d_r2c(None, None) == capi.HPXFFT_ERR_STATE
+    assert lib.hpxfft_plan3d_buffer_bytes(None, ctypes.byref(n)) == capi.HPXFFT_ERR_INVALID_ARG
+    assert lib.hpxfft_plan3d_get_measurement(None, b"total", ctypes.byref(v)) == capi.HPXFFT_ERR_INVALID_ARG
+
+
 @pytest.fixture(scope="module")
 def ffhost(tmp_path_factory):
     cxx = shutil.which("g++")
