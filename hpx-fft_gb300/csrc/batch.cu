@@ -530,7 +530,8 @@ int hpxfft_wisdom_import(const char *path)
     std::vector<char> buf(1 << 16);
     char *key = buf.data();
     Tuning t;
-    while (fscanf(f, "%65535s %d %d", key, &t.lag, &t.ctas_per_sm) == 3) {
+    int got;
+    while ((got = fscanf(f, "%65535s %d %d", key, &t.lag, &t.ctas_per_sm)) == 3) {
         if (t.lag < 0 || t.lag > 4096 || t.ctas_per_sm < 1 || t.ctas_per_sm > 8) {
             fclose(f);
             return set_error(HPXFFT_ERR_INVALID_ARG, "corrupt wisdom entry");
@@ -538,6 +539,9 @@ int hpxfft_wisdom_import(const char *path)
         rows.push_back({key, t});
     }
     fclose(f);
+    // only a clean end of file ends the entries: a truncated or unparsable
+    // entry rejects the whole file, and nothing of it is merged
+    if (got != EOF) return set_error(HPXFFT_ERR_INVALID_ARG, "corrupt wisdom entry");
     std::lock_guard<std::mutex> lock(g_cache_mu);
     for (auto &r : rows) g_cache[r.first] = r.second;
     return HPXFFT_OK;

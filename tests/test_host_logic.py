@@ -169,3 +169,58 @@ def test_distributed_comm_flag_is_validated(gpu_lib):
     v = gpu_lib.util.vector_2d(4, 6, 0.0)
     with pytest.raises(gpu_lib.HpxFftInvalidArgument, match="scatter or all_to_all"):
         gpu_lib.distributed.loop().initialize(v, "broadcast", "estimate")
+
+
+def test_wisdom_file_round_trip_and_corrupt_files(gpu_lib, tmp_path):
+    """The tuned-plan cache file (host only): import then export gives the
+    same entries, sorted by key; a corrupt file is rejected whole and
+    merges nothing; unopenable paths raise the I/O status, like
+    loop::write_plans_to_file's std::runtime_error (core/src/shared/loop.cpp:197-201)."""
+    from hpxfft import batch as hb
+
+    capi = gpu_lib._capi
+    head = "hpxfft-gb300-wisdom 1\n"
+    entries = ["p2;512x642*3 16 3", "p2;256x514*8;384x258*8 8 2", "p0;64x66*1 0 1"]
+    good = tmp_path / "good.txt"
+    good.write_text(head + "\n".join(entries) + "\n")
+    out = tmp_path / "out.txt"
+
+    def exported():
+        hb.wisdom_export(str(out))
+        lines = out.read_text().splitlines()
+        assert lines[0] == head.strip()
+        return lines[1:]
+
+    hb.wisdom_forget()
+    try:
+        assert exported() == []
+        hb.wisdom_import(str(good))
+        assert exported() == sorted(entries)
+        corrupt = {
+            "header": "not wisdom\n",
+            "version": "hpxfft-gb300-wisdom 2\n",
+            "lag range": head + "k 5000 2\n",
+            "negative lag": head + "k -1 2\n",
+            "ctas low": head + "k 8 0\n",
+            "ctas high": head + "k 8 9\n",
+            "truncated": head + "k1 8 2\nk2 8",
+            "not a number": head + "k eight 2\n",
+            "trailing junk": head + "k1 8 2\njunk\n",
+        }
+        for name, text in corrupt.items():
+            bad = tmp_path / "bad.txt"
+            bad.write_text(text)
+            with pytest.raises(gpu_lib.HpxFftInvalidArgument):
+                hb.wisdom_import(str(bad))
+            assert exported() == sorted(entries), name
+        empty = tmp_path / "empty.txt"
+        empty.write_text(head)
+        hb.wisdom_import(str(empty))
+        assert exported() == sorted(entries)
+        for call in (lambda: hb.wisdom_import(str(tmp_path / "missing.txt")),
+                     lambda: hb.wisdom_export(str(tmp_path))):
+            with pytest.raises(gpu_lib.HpxFftError) as e:
+                call()
+            assert e.value.status == capi.HPXFFT_ERR_IO
+    finally:
+        hb.wisdom_forget()
