@@ -224,3 +224,30 @@ def test_wisdom_file_round_trip_and_corrupt_files(gpu_lib, tmp_path):
             assert e.value.status == capi.HPXFFT_ERR_IO
     finally:
         hb.wisdom_forget()
+
+
+def test_last_error_is_per_thread(gpu_lib):
+    """hpxfft_last_error reports the calling thread's own failure while
+    another thread fails differently in between (one host thread per handle,
+    handles used concurrently)."""
+    import threading
+
+    lib = gpu_lib._capi.load()
+    cases = [((4, 6, 1, 0, b"wisdom"), b"plan flag"), ((4, 5, 1, 0, b"estimate"), b"n_col must be")]
+    start = threading.Barrier(len(cases))
+    wrong = []
+
+    def worker(args, expect):
+        h = ctypes.c_void_p()
+        start.wait()
+        for _ in range(2000):
+            assert lib.hpxfft_plan_create(ctypes.byref(h), *args) != gpu_lib._capi.HPXFFT_OK
+            if expect not in lib.hpxfft_last_error():
+                wrong.append(expect)
+
+    threads = [threading.Thread(target=worker, args=c) for c in cases]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not wrong, wrong[:3]
