@@ -99,6 +99,7 @@ def build_oracle(force: bool = False) -> str:
 CPP_PROGRAMS = {
     # the drop-in C++ API: the reference's tests and its shared-loop driver
     "test_dropin": os.path.join(REPO, "tests", "cpp", "test_dropin.cpp"),
+    "test_dropin_host": os.path.join(REPO, "tests", "cpp", "test_dropin_host.cpp"),
     "hpxfft_gpu_shared_loop": os.path.join(PKG_DIR, "examples", "shared_loop_2d.cpp"),
 }
 

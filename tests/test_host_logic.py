@@ -251,3 +251,13 @@ def test_last_error_is_per_thread(gpu_lib):
     for t in threads:
         t.join()
     assert not wrong, wrong[:3]
+
+
+def test_cpp_dropin_host_side(gpu_lib, build_mod, tmp_path):
+    """What the C++ drop-in classes decide before a plan touches the device
+    (exception types, unknown measurement keys, vector_2d ownership),
+    compiled against the drop-in headers; runs without a GPU."""
+    exe = build_mod.build_cpp()["test_dropin_host"]
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120, cwd=tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "all host-side drop-in checks passed" in r.stdout
