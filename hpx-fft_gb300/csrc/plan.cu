@@ -725,6 +725,11 @@ static int create_plan(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
     if (n_col < 4 || n_col % 2) return fail(HPXFFT_ERR_UNSUPPORTED_SIZE, "n_col must be 2*(ny/2+1) with ny >= 2 even");
     if (n_row > (1u << 30) || n_col > (1u << 30) || batch > 65535)
         return fail(HPXFFT_ERR_UNSUPPORTED_SIZE, "dimension too large");
+    // the split-BF16 column steps need nx = N1 * N2 with N1, N2 in
+    // {32, 64, 128, 256}: the same condition plan_colsteps applies below,
+    // checked here before anything touches the device
+    if (precision == HPXFFT_PREC_BF16X3 && (n_row < 1024 || n_row > 65536 || (n_row & (n_row - 1))))
+        return fail(HPXFFT_ERR_UNSUPPORTED_SIZE, "split-BF16 precision needs n_row a power of two in [1024, 65536]");
     const auto t0 = std::chrono::steady_clock::now();
     hpxfft_plan_s *p = new (std::nothrow) hpxfft_plan_s();
     if (!p) return fail(HPXFFT_ERR_ALLOC, "host allocation failed");
