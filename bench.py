@@ -174,6 +174,30 @@ def cpu_baseline(nx: int, ny: int, host_input: np.ndarray, threads: int) -> dict
     }
 
 
+def pocketfft_context(nx: int, ny: int, host_input: np.ndarray, threads: int):
+    """scipy.fft.rfft2 (pocketfft, FP64) of the same input on the same host
+    cores: a production CPU FFT beside the restatement, since FFTW (the
+    reference's FFT library) is not installed.  Context only, timed outside
+    every timed region; None when scipy is missing or the run fails."""
+    try:
+        import scipy.fft
+
+        x = np.ascontiguousarray(host_input[:, :ny])
+        t0 = time.perf_counter()
+        out = scipy.fft.rfft2(x, workers=threads)
+        dt = time.perf_counter() - t0
+        del out, x
+    except Exception:
+        return None
+    return {
+        "value": algorithmic_bytes(nx, ny, 8) / dt / 1e9,
+        "unit": UNIT,
+        "cores": threads,
+        "sample": f"one {nx}x{ny} FP64 scipy.fft.rfft2 ({dt:.2f} s, workers={threads}): pocketfft standing in "
+                  f"for FFTW, which is not installed",
+    }
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -242,6 +266,9 @@ def run_reference(args):
                          "sample": f"{args.steps} full {nx}x{ny} FP64 transforms, {threads} threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    pocket = pocketfft_context(nx, ny, x, threads)
+    if pocket is not None:
+        line["cpu_pocketfft"] = pocket
     print(json.dumps(line), flush=True)
     return 0
 
@@ -353,6 +380,7 @@ def run_ours(args):
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
             cpu = cpu_baseline(nx, ny, x64, threads)
+            pocket = pocketfft_context(nx, ny, x64, threads)
             ref = x64.copy()
             oracle.fft_2d_r2c(ref, nthreads=threads)
             refc = ref.view(np.complex128)
@@ -416,6 +444,8 @@ def run_ours(args):
         }
         if cpu is not None:
             line["cpu_baseline"] = {k: v for k, v in cpu.items() if k != "seconds"}
+            if pocket is not None:
+                line["cpu_pocketfft"] = pocket
         if not args.no_extras and world == 1:
             line["extras"] = extras(torch, hpxfft, args, x64, oracle_ref if cpu is not None else None, peak)
         print(json.dumps(line), flush=True)
