@@ -1,11 +1,14 @@
-"""CPU-only checks: the C ABI library loads and exports its header, argument
-validation that never touches the GPU, the float-float conversions compiled
-for the host, and the Python mirror of vector_2d."""
+"""CPU-only checks: the C ABI library loads and exports its header; argument
+and size validation that never touches the GPU (2D, 3D, the planner's size
+limits, the C++ drop-in classes); per-thread error messages; the wisdom
+file; no fallback when the library is absent; the float-float conversions
+compiled for the host; and the Python mirror of vector_2d."""
 import ctypes
 import os
 import re
 import shutil
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -290,3 +293,33 @@ def test_planner_size_limits_before_any_device_call(gpu_lib):
         assert status(*shape) != capi.HPXFFT_ERR_UNSUPPORTED_SIZE, shape
     for shape in rejected:
         assert status(*shape) == capi.HPXFFT_ERR_UNSUPPORTED_SIZE, shape
+
+
+def test_every_entry_point_fails_loudly_without_the_library(tmp_path):
+    """No CPU fallback: with the native library absent, each public entry
+    point raises instead of computing anything (fresh interpreter, so no
+    library is loaded yet)."""
+    code = f"""
+import sys
+sys.path.insert(0, {os.path.join(REPO, 'hpx-fft_gb300', 'python')!r})
+import hpxfft
+hpxfft._capi.LIB_PATH = {str(tmp_path / 'absent' / 'libhpxfft_gb300.so')!r}
+calls = {{
+    "Plan": lambda: hpxfft.Plan(4, 6),
+    "Plan3D": lambda: hpxfft.Plan3D(4, 4, 6),
+    "Batch": lambda: hpxfft.Batch([8], [10], "f32"),
+    "shared.loop": lambda: hpxfft.shared.loop().initialize(hpxfft.util.vector_2d(4, 6, 0.0), "estimate"),
+    "plan_flag_valid": lambda: hpxfft.plan.plan_flag_valid("estimate"),
+    "wisdom_forget": lambda: hpxfft.batch.wisdom_forget(),
+}}
+for name, call in calls.items():
+    try:
+        call()
+    except OSError as e:
+        assert "no CPU fallback" in str(e), (name, e)
+    else:
+        raise SystemExit(name + " ran without the library")
+print("all raised")
+"""
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and "all raised" in r.stdout, r.stdout + r.stderr
