@@ -63,6 +63,13 @@ typedef struct hpxfft_plan3d_s *hpxfft_plan3d;
  * (n_col = 2*(ny/2+1), so ny = n_col - 2).  plan_flag is one of
  * "estimate", "measure", "patient", "exhaustive"; anything else returns
  * HPXFFT_ERR_INVALID_ARG.  Allocates the twiddle tables and no data buffer.
+ * Sizes: ny even; ny/2 (the row's complex length) and n_row without a prime
+ * factor above 13.  A row runs on a cluster of C in {1, 2, 4} CTAs of at
+ * most 8192 complex values each, a column on C in {1, 2, 4, 8, 16} CTAs of
+ * at most 4096 (FP64) or 8192 (FP32) each; C > 1 needs the length
+ * divisible by C^2.  So ny <= 65536 and n_row <= 65536 (FP64) or 131072
+ * (FP32).  batch <= 65535.  Other sizes return HPXFFT_ERR_UNSUPPORTED_SIZE
+ * before any device call.
  * Replaces: hpxfft::shared::loop::initialize (core/src/shared/loop.cpp:158-189)
  * and fftw_adapter::{r2c_1d,c2c_1d}::plan (core/src/util/adapter_fftw.cpp:6-10,24-30),
  * string_to_fftw_plan_flag (core/include/hpxfft/util/adapter_fftw.hpp:22-44). */
