@@ -327,3 +327,18 @@ print("all raised")
 """
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and "all raised" in r.stdout, r.stdout + r.stderr
+
+
+def test_cli_driver_rejects_bad_options_without_a_gpu(gpu_lib, build_mod, tmp_path):
+    """hpxfft_gpu_shared_loop: an unknown option exits 2; a bad --plan ends
+    the process with the std::invalid_argument of string_to_fftw_plan_flag
+    (core/include/hpxfft/util/adapter_fftw.hpp:42) uncaught, as the
+    reference's driver does (examples/hpxfft/shared_loop_2d.cpp:46); no
+    output files are written in either case."""
+    exe = build_mod.build_cpp()["hpxfft_gpu_shared_loop"]
+    r = subprocess.run([exe, "--nx=4", "--threads=8"], capture_output=True, text=True, timeout=60, cwd=tmp_path)
+    assert r.returncode == 2 and "unknown option --threads" in r.stderr
+    r = subprocess.run([exe, "--nx", "4", "--ny", "6", "--plan=fastest"], capture_output=True, text=True,
+                       timeout=60, cwd=tmp_path)
+    assert r.returncode != 0 and "Invalid FFTW plan flag string" in r.stderr
+    assert not (tmp_path / "runtimes").exists() and not (tmp_path / "plans").exists()
