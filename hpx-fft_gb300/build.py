@@ -135,7 +135,98 @@ def build_all(force: bool = False) -> None:
     build_cpp(force)
 
 
+def resource_report(pattern: str | None = None) -> str:
+    """Registers, spills and static shared memory of every kernel and
+    non-inlined device function, as ptxas reports them (-Xptxas -v), grouped
+    by function name: a markdown table, then one row per instance whose
+    demangled name matches the regular expression `pattern`.  Compiles into
+    a temporary folder; the library build is untouched."""
+    import re
+    import tempfile
+    from collections import defaultdict
+
+    nvcc = _nvcc()
+    kernel_sources = [s for s in SOURCES if s.startswith("kernels_") or s == "batch.cu"]
+    with tempfile.TemporaryDirectory() as tmp:
+        cmds = [[nvcc, *ARCH, *NVCC_FLAGS, "-Xptxas", "-v", "-c", os.path.join(CSRC, s), "-o",
+                 os.path.join(tmp, s + ".o")] for s in kernel_sources]
+
+        def run(cmd):
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"command failed: {' '.join(cmd)}\n{r.stderr}")
+            return r.stderr
+
+        with ThreadPoolExecutor(max_workers=len(cmds)) as ex:
+            logs = list(ex.map(run, cmds))
+    funcs = {}
+    cur = None
+    for line in "\n".join(logs).splitlines():
+        m = re.search(r"Function properties for (\S+)", line)
+        if m:
+            cur = funcs.setdefault(m.group(1), {"regs": 0, "spill": 0, "stack": 0, "smem": 0})
+            continue
+        m = re.search(r"(\d+) bytes stack frame, (\d+) bytes spill stores, (\d+) bytes spill loads", line)
+        if m and cur is not None:
+            cur["stack"] = int(m.group(1))
+            cur["spill"] = int(m.group(2)) + int(m.group(3))
+            continue
+        m = re.search(r"Compiling entry function '(\S+)'", line)
+        if m:
+            cur = funcs.setdefault(m.group(1), {"regs": 0, "spill": 0, "stack": 0, "smem": 0})
+            continue
+        m = re.search(r"Used (\d+) registers.*?(?:(\d+) bytes smem)?,", line)
+        if m and cur is not None:
+            cur["regs"] = int(m.group(1))
+            s = re.search(r"(\d+) bytes smem", line)
+            cur["smem"] = int(s.group(1)) if s else 0
+    names = list(funcs)
+    filt = shutil.which("c++filt")
+    if filt:
+        out = subprocess.run([filt], input="\n".join(names), capture_output=True, text=True).stdout.splitlines()
+        if len(out) == len(names):
+            names = out
+    groups = defaultdict(list)
+    for pretty, rec in zip(names, funcs.values()):
+        base = pretty.split("(")[0]
+        base = re.sub(r"^void ", "", base).split("<")[0].split("::")[-1]
+        groups[base].append((pretty, rec))
+    rows = ["| function | instances | registers (min-max) | static smem B (max) | stack B (max) | spill B (max) |",
+            "|---|---|---|---|---|---|"]
+    for base in sorted(groups):
+        recs = [r for _, r in groups[base]]
+        regs = [r["regs"] for r in recs]
+        rows.append(f"| `{base}` | {len(recs)} | {min(regs)}-{max(regs)} | {max(r['smem'] for r in recs)} | "
+                    f"{max(r['stack'] for r in recs)} | {max(r['spill'] for r in recs)} |")
+    spilled = [(p, r) for b in groups for p, r in groups[b] if r["spill"]]
+    rows.append("")
+    rows.append(f"{len(funcs)} functions; {len(spilled)} with spills.")
+    if spilled:
+        # instances whose compiled length (third template argument, or the
+        # batch bodies' first) is 0 choose their radices at plan time
+        where = defaultdict(list)
+        for p, r in spilled:
+            base = re.sub(r"^void ", "", p.split("(")[0]).split("<")[0].split("::")[-1]
+            runtime = re.search(r", 0, 0>", p) is not None
+            where[(base, "runtime-planned (compiled length 0)" if runtime else "compiled shapes")].append(r["spill"])
+        rows += ["", "| function | instances | which | spill B (min-max) |", "|---|---|---|---|"]
+        for (base, kind), v in sorted(where.items()):
+            rows.append(f"| `{base}` | {len(v)} | {kind} | {min(v)}-{max(v)} |")
+    if pattern:
+        rows += ["", "| instance | registers | static smem B | stack B | spill B |", "|---|---|---|---|---|"]
+        for b in sorted(groups):
+            for p, r in groups[b]:
+                if re.search(pattern, p):
+                    name = p.replace("hpxfft_gpu::", "").replace("void ", "")
+                    rows.append(f"| `{name[:150]}` | {r['regs']} | {r['smem']} | {r['stack']} | {r['spill']} |")
+    return "\n".join(rows)
+
+
 if __name__ == "__main__":
+    if "--resources" in sys.argv:
+        i = sys.argv.index("--resources")
+        print(resource_report(sys.argv[i + 1] if i + 1 < len(sys.argv) else None))
+        sys.exit(0)
     build_all(force="--force" in sys.argv)
     print(LIB)
     print(ORACLE_LIB)
