@@ -342,3 +342,19 @@ def test_cli_driver_rejects_bad_options_without_a_gpu(gpu_lib, build_mod, tmp_pa
                        timeout=60, cwd=tmp_path)
     assert r.returncode != 0 and "Invalid FFTW plan flag string" in r.stderr
     assert not (tmp_path / "runtimes").exists() and not (tmp_path / "plans").exists()
+
+
+def test_c_abi_from_plain_c(gpu_lib, tmp_path):
+    """The header compiles as strict C99 and a C program links the library
+    and gets the host-side statuses: what a cgo / JNI / N-API binding needs."""
+    cc = shutil.which("gcc")
+    if not cc:
+        pytest.skip("gcc not available")
+    lib_dir = os.path.dirname(gpu_lib._capi.LIB_PATH)
+    exe = tmp_path / "abi_host_check"
+    src = os.path.join(REPO, "tests", "c", "abi_host_check.c")
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", f"-I{os.path.join(REPO, 'include')}",
+                    "-o", str(exe), src, f"-L{lib_dir}", "-lhpxfft_gb300", f"-Wl,-rpath,{lib_dir}"], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "all C ABI host checks passed" in r.stdout
