@@ -62,7 +62,11 @@ typedef struct hpxfft_plan3d_s *hpxfft_plan3d;
 /* Plan a 2D r2c of `batch` equally sized arrays of n_row x n_col reals
  * (n_col = 2*(ny/2+1), so ny = n_col - 2).  plan_flag is one of
  * "estimate", "measure", "patient", "exhaustive"; anything else returns
- * HPXFFT_ERR_INVALID_ARG.  Allocates the twiddle tables and no data buffer.
+ * HPXFFT_ERR_INVALID_ARG.  Every valid flag plans the same 2D transform (the
+ * kernel, column strategy and launch shapes are fixed rules set by
+ * measurements on GB300), so planning never runs trial transforms; the
+ * batch plan is where "measure" and stronger flags time candidates.
+ * Allocates the twiddle tables and no data buffer.
  * Sizes: ny even; ny/2 (the row's complex length) and n_row without a prime
  * factor above 13.  A row runs on a cluster of C in {1, 2, 4} CTAs of at
  * most 8192 complex values each, a column on C in {1, 2, 4, 8, 16} CTAs of
