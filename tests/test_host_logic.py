@@ -358,3 +358,19 @@ def test_c_abi_from_plain_c(gpu_lib, tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "all C ABI host checks passed" in r.stdout
+
+
+def test_batch_argument_errors_before_any_device_call(gpu_lib):
+    """The batch plan rejects bad flags, shapes and precisions on the host."""
+    capi = gpu_lib._capi
+    invalid = [([8], [10], "f32", "fast"), ([], [], "f32"), ([8], [10], "bf16x3"), ([8, 8], [10], "f32")]
+    for args in invalid:
+        with pytest.raises(gpu_lib.HpxFftInvalidArgument):
+            gpu_lib.Batch(*args)
+    unsupported = [([8, 17], [10, 10], "f32"),  # 17 rows: a prime above 13
+                   ([16384], [10], "f32"),      # a column must fit one CTA
+                   ([8], [9], "f32")]           # odd n_col
+    for args in unsupported:
+        with pytest.raises(gpu_lib.HpxFftError) as e:
+            gpu_lib.Batch(*args)
+        assert e.value.status == capi.HPXFFT_ERR_UNSUPPORTED_SIZE, args
