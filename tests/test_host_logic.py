@@ -161,6 +161,12 @@ def test_vector_2d_mirror(gpu_lib):
     assert vec.n_row() == 3 and vec.n_col() == 3 and vec(0, 0) == 4.0 and vec(2, 2) == 4.0 and vec.size() == 9
     with pytest.raises(RuntimeError):
         v2(3, 3, 1.0).at(3, 3)
+    # like the reference (vector_2d.hpp:218-221), at() bounds the flat index
+    # i * n_col + j only: (0, 3) is element 3, i.e. (1, 0)
+    vec[1, 0] = 7.0
+    assert vec.at(0, 3) == 7.0
+    with pytest.raises(RuntimeError):
+        vec.at(2, 3)
     assert v2(2, 2, 5.0) == v2(2, 2, 5.0)
     assert not (v2(2, 2, 5.0) == v2(2, 2, 6.0))
     moved = v2(2, 4, 1.0)
