@@ -1,8 +1,9 @@
-"""CPU-only checks: the C ABI library loads and exports its header; argument
-and size validation that never touches the GPU (2D, 3D, the planner's size
-limits, the C++ drop-in classes); per-thread error messages; the wisdom
-file; no fallback when the library is absent; the float-float conversions
-compiled for the host; and the Python mirror of vector_2d."""
+"""CPU-only checks: the C ABI library loads and exports its header, and links
+from plain C99; argument and size validation that never touches the GPU (2D,
+3D and batch plans, the planner's size limits, the C++ drop-in classes, the
+CLI driver); per-thread error messages; the wisdom file; no fallback when
+the library is absent; the float-float conversions compiled for the host;
+and the Python mirror of vector_2d."""
 import ctypes
 import os
 import re
