@@ -80,6 +80,11 @@ def workload_input(nx: int, ny: int, seed: int = 1234) -> np.ndarray:
     return x
 
 
+def workload_name(nx: int, ny: int, prec: str = "f64") -> str:
+    """The workload label both arms print (same transform, size and input)."""
+    return f"2d_r2c_{prec}_{nx}x{ny}"
+
+
 def algorithmic_bytes(nx: int, ny: int, real_bytes: int) -> float:
     S = nx * (ny // 2 + 1) * 2 * real_bytes
     return 4.0 * S
@@ -260,7 +265,7 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic: uniform[-1,1) + 4 integer-frequency sinusoids of amplitude 10, seed 1234",
-        "config": {"workload": f"2d_r2c_fp64_{nx}x{ny}", "nx": nx, "ny": ny, "layout": "padded in-place vector_2d",
+        "config": {"workload": workload_name(nx, ny), "nx": nx, "ny": ny, "layout": "padded in-place vector_2d",
                    "implementation": "C restatement of hpxfft::shared::loop (FFTW/HPX unavailable)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} full {nx}x{ny} FP64 transforms, {threads} threads"},
@@ -400,7 +405,7 @@ def run_ours(args):
             "dtype": "f32" if f32 else "f64",
             "data": "synthetic: uniform[-1,1) + 4 integer-frequency sinusoids of amplitude 10, seed 1234+rank",
             "config": {
-                "workload": f"2d_r2c_{prec}_{nx}x{ny}",
+                "workload": workload_name(nx, ny, prec),
                 "nx": nx, "ny": ny,
                 "precision": {"f64": "FP64 storage, float-float arithmetic", "f32": "FP32",
                               "bf16x3": "FP32 storage, split-BF16 tensor-core column stage",
@@ -529,6 +534,36 @@ def batch_workload(torch, hpxfft, stream, count, flag, steps, warm, peak):
     return res
 
 
+def _rel_to_oracle(got, oracle_ref):
+    d = got.astype(np.complex128) - oracle_ref
+    return float(np.linalg.norm(d.ravel()) / np.linalg.norm(oracle_ref.ravel())), float(np.abs(d).max())
+
+
+def cufft_side(torch, stream, x64, nx, ny, steps, warm, oracle_ref, peak):
+    """cuFFT (through torch.fft.rfft2, out of place, unpadded input) on the
+    same input in FP64 and FP32: a GPU library timed beside the product for
+    context, never called by it.  value uses the same 4 S bytes as the
+    product's lines."""
+    res = {"library": f"cuFFT via torch.fft.rfft2 (torch {torch.__version__})"}
+    for prec, dt, rb in (("f64", torch.float64, 8), ("f32", torch.float32, 4)):
+        x = torch.from_numpy(np.ascontiguousarray(x64[:, :ny], dtype=np.float64 if rb == 8 else np.float32)).cuda()
+        holder = {}
+
+        def step():
+            holder["y"] = torch.fft.rfft2(x)
+
+        ms = _time_steps(torch, stream, step, steps, warm)
+        B = algorithmic_bytes(nx, ny, rb)
+        sec = {"ms": ms, "value": B / (ms * 1e-3) / 1e9, "unit": "GB/s", "frac_of_measured_hbm": B / (ms * 1e-3) / 1e9 / peak}
+        if oracle_ref is not None:
+            sec["rel_l2_vs_fp64_oracle"], sec["max_abs_err_vs_fp64_oracle"] = _rel_to_oracle(
+                holder["y"].cpu().numpy(), oracle_ref)
+        res[prec] = sec
+        del x, holder
+        torch.cuda.empty_cache()
+    return res
+
+
 def extras(torch, hpxfft, args, x64, oracle_ref, peak):
     """The other workloads of this path, measured in the same run:
     FP32 at the same size (precision), 1024 uneven FP32 transforms in one
@@ -539,6 +574,30 @@ def extras(torch, hpxfft, args, x64, oracle_ref, peak):
     nx, ny = args.nx, args.ny
     nc = 2 * (ny // 2 + 1)
     steps, warm = max(3, args.steps), max(3, args.warmup)
+
+    # the FP64 transform with native DFMA arithmetic instead of float-float
+    # (HPXFFT_PREC_F64_NATIVE, runtime-planned kernels): the alternative the
+    # float-float design is measured against
+    xin = torch.from_numpy(x64).cuda()
+    xout = torch.empty_like(xin)
+    with hpxfft.Plan(nx, nc, 1, "f64-native", "estimate") as pn:
+        pn.set_stream(stream.cuda_stream)
+        ms = _time_steps(torch, stream, lambda: pn.execute_oop(xin.data_ptr(), xout.data_ptr()), 3, 1)
+        pn.synchronize()
+        B = algorithmic_bytes(nx, ny, 8)
+        sec = {"workload": workload_name(nx, ny, "f64-native"), "ms": ms, "value": B / (ms * 1e-3) / 1e9,
+               "unit": "GB/s", "frac_of_measured_hbm": B / (ms * 1e-3) / 1e9 / peak}
+        if oracle_ref is not None:
+            sec["rel_l2_vs_fp64_oracle"], sec["max_abs_err_vs_fp64_oracle"] = _rel_to_oracle(
+                xout.cpu().numpy().view(np.complex128), oracle_ref)
+        out["precision_f64_native"] = sec
+    del xin, xout
+    torch.cuda.empty_cache()
+    out["cufft_side_comparison"] = cufft_side(torch, stream, x64, nx, ny, steps, warm, oracle_ref, peak)
+    try:
+        out["pipe_peaks"] = hpxfft.pipe_peaks()
+    except Exception as exc:  # the measurement is context, not part of the step
+        out["pipe_peaks"] = {"error": str(exc)}
 
     # precision: FP32 in and out (CUDA cores, and with the split-BF16 tensor-core
     # column stage), error against the FP64 oracle
@@ -552,16 +611,14 @@ def extras(torch, hpxfft, args, x64, oracle_ref, peak):
             ms = _time_steps(torch, stream, lambda: p32.execute_oop(x32.data_ptr(), y32.data_ptr()), steps, warm)
             p32.synchronize()
             B = algorithmic_bytes(nx, ny, 4)
-            sec = {"workload": f"2d_r2c_{prec}_{nx}x{ny}", "ms": ms, "value": B / (ms * 1e-3) / 1e9, "unit": "GB/s",
+            sec = {"workload": workload_name(nx, ny, prec), "ms": ms, "value": B / (ms * 1e-3) / 1e9, "unit": "GB/s",
                    "frac_of_measured_hbm": B / (ms * 1e-3) / 1e9 / peak}
             if prec == "bf16x3":
                 sec["tensor_core_stage"] = ("first radix-16 pass of the rows and of both column steps, tcgen05 "
                                             "kind::f16, 3-term BF16 split, FP32 accumulate")
             if oracle_ref is not None:
-                got = y32.cpu().numpy().view(np.complex64).astype(np.complex128)
-                d = got - oracle_ref
-                sec["rel_l2_vs_fp64_oracle"] = float(np.linalg.norm(d.ravel()) / np.linalg.norm(oracle_ref.ravel()))
-                sec["max_abs_err_vs_fp64_oracle"] = float(np.abs(d).max())
+                sec["rel_l2_vs_fp64_oracle"], sec["max_abs_err_vs_fp64_oracle"] = _rel_to_oracle(
+                    y32.cpu().numpy().view(np.complex64), oracle_ref)
             out[f"precision_{prec}"] = sec
     del x32, y32
 

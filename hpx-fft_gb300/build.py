@@ -34,6 +34,7 @@ SOURCES = [
     "twiddles.cu",
     "plan.cu",
     "batch.cu",
+    "pipe_peaks.cu",
 ]
 
 

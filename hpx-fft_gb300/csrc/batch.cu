@@ -6,6 +6,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -21,6 +22,11 @@ namespace hpxfft_gpu {
 
 // plan.cu: records the calling thread's error message, returns status
 int set_error(int status, const std::string &msg);
+// plan.cu: the 2D plans' cached choices in wisdom files
+void wisdom2d_write(FILE *f);
+bool wisdom2d_check(const std::string &key, const std::vector<long long> &v);
+void wisdom2d_add(const std::string &key, const std::vector<long long> &v);
+void wisdom2d_forget();
 
 namespace {
 
@@ -68,21 +74,6 @@ std::string cache_key(const std::vector<size_t> &nr, const std::vector<size_t> &
     return k;
 }
 
-bool factor_plan(int L, PassPlan &pp)
-{
-    int odd[kMaxPasses], nodd = 0, rest = L;
-    for (int q : {3, 5, 7, 11, 13})
-        while (rest % q == 0 && nodd < kMaxPasses) rest /= q, odd[nodd++] = q;
-    if (rest & (rest - 1)) return false;
-    int p2 = 0;
-    while ((1 << p2) < rest) ++p2;
-    pp.n = 0;
-    while (p2 >= 4 && pp.n < kMaxPasses) pp.radix[pp.n++] = 16, p2 -= 4;
-    if (p2 > 0 && pp.n < kMaxPasses) pp.radix[pp.n++] = 1 << p2;
-    for (int i = 0; i < nodd && pp.n < kMaxPasses; ++i) pp.radix[pp.n++] = odd[i];
-    return pp.n < kMaxPasses;
-}
-
 }  // namespace
 }  // namespace hpxfft_gpu
 
@@ -95,6 +86,8 @@ struct hpxfft_batch_s {
     std::vector<size_t> offsets_bytes;
     size_t arena_bytes = 0;
     hpxfft_gpu::Tuning tune;
+    // polls of a column item's bounded wait for its instance's rows
+    long long spin_limit = 1ll << 24;
     // device tables
     hpxfft_gpu::BatchInst *d_insts = nullptr;
     hpxfft_gpu::BatchItem *d_items = nullptr;
@@ -127,7 +120,7 @@ cudaError_t launch_batch(hpxfft_batch_s &b, void *arena, cudaStream_t st)
     a.twpool = b.d_tw;
     a.nitems = (int)b.items.size();
     a.counters = b.d_counters;
-    a.spin_limit = 1ll << 24;
+    a.spin_limit = b.spin_limit;
     batch_kernel<A><<<b.grid, kBatchThreads, (size_t)padded_elems(b.prec == HPXFFT_PREC_F32 ? 8192 : 4096) * 2 *
                                                     b.real_bytes,
                       st>>>(a);
@@ -202,6 +195,15 @@ int hpxfft_batch_create(hpxfft_batch *out, size_t count, const size_t *n_rows, c
     if (!b) return set_error(HPXFFT_ERR_ALLOC, "host allocation");
     b->prec = precision;
     b->real_bytes = precision == HPXFFT_PREC_F32 ? 4 : 8;
+    // HPXFFT_BATCH_SPIN_LIMIT=n lowers the bound of the column items' wait
+    // (n polls of 128 ns each), so a test can make it run out: the kernel
+    // then skips the item and hpxfft_batch_synchronize reports
+    // HPXFFT_ERR_TIMEOUT; the kernel returns either way
+    if (const char *env = std::getenv("HPXFFT_BATCH_SPIN_LIMIT")) {
+        char *end = nullptr;
+        const long long v = std::strtoll(env, &end, 10);
+        if (end != env && v >= 0) b->spin_limit = v;
+    }
     const int maxel = precision == HPXFFT_PREC_F32 ? 8192 : 4096;
     const int cbytes = 2 * (int)b->real_bytes;
     std::map<std::tuple<int, int, int>, int> dim_index;  // (kind, L, log2W) -> dims
@@ -225,7 +227,7 @@ int hpxfft_batch_create(hpxfft_batch *out, size_t count, const size_t *n_rows, c
         auto it = dim_index.find({kind, L, lw});
         if (it != dim_index.end()) return it->second;
         BatchDim d{};
-        if (!factor_plan(L, d.pp)) return -1;
+        if (!factorize_radices(L, d.pp)) return -1;
         d.L = L;
         d.log2W = lw;
         d.fixed_id = fixed_id(kind, L, lw);
@@ -508,49 +510,92 @@ int hpxfft_wisdom_export(const char *path)
     if (!path) return set_error(HPXFFT_ERR_INVALID_ARG, "null path");
     FILE *f = fopen(path, "w");
     if (!f) return set_error(HPXFFT_ERR_IO, std::string("Failed to open file: ") + path);
-    std::lock_guard<std::mutex> lock(g_cache_mu);
-    fprintf(f, "hpxfft-gb300-wisdom 1\n");
-    for (auto &kv : g_cache) fprintf(f, "%s %d %d\n", kv.first.c_str(), kv.second.lag, kv.second.ctas_per_sm);
+    fprintf(f, "hpxfft-gb300-wisdom 2\n");
+    {
+        std::lock_guard<std::mutex> lock(g_cache_mu);
+        for (auto &kv : g_cache) fprintf(f, "%s %d %d\n", kv.first.c_str(), kv.second.lag, kv.second.ctas_per_sm);
+    }
+    wisdom2d_write(f);
     fclose(f);
     return HPXFFT_OK;
 }
 
+// Version 1 files hold batch entries ("key lag ctas_per_sm"); version 2 adds
+// 2D plan entries ("2d;... columns ff_pairs tc_vectors tc_rows").  A file
+// with any malformed entry is rejected whole: nothing of it is merged.
 int hpxfft_wisdom_import(const char *path)
 {
     if (!path) return set_error(HPXFFT_ERR_INVALID_ARG, "null path");
     FILE *f = fopen(path, "r");
     if (!f) return set_error(HPXFFT_ERR_IO, std::string("Failed to open file: ") + path);
-    char head[64] = {};
-    int version = 0;
-    if (fscanf(f, "%63s %d", head, &version) != 2 || strcmp(head, "hpxfft-gb300-wisdom") || version != 1) {
-        fclose(f);
-        return set_error(HPXFFT_ERR_INVALID_ARG, "not a wisdom file");
-    }
-    std::vector<std::pair<std::string, Tuning>> rows;
-    std::vector<char> buf(1 << 16);
-    char *key = buf.data();
-    Tuning t;
-    int got;
-    while ((got = fscanf(f, "%65535s %d %d", key, &t.lag, &t.ctas_per_sm)) == 3) {
-        if (t.lag < 0 || t.lag > 4096 || t.ctas_per_sm < 1 || t.ctas_per_sm > 8) {
-            fclose(f);
-            return set_error(HPXFFT_ERR_INVALID_ARG, "corrupt wisdom entry");
+    std::vector<std::string> lines;
+    {
+        std::string cur;
+        int ch;
+        while ((ch = fgetc(f)) != EOF) {
+            if (ch == '\n') {
+                lines.push_back(cur);
+                cur.clear();
+            } else {
+                cur.push_back((char)ch);
+            }
         }
-        rows.push_back({key, t});
+        if (!cur.empty()) lines.push_back(cur);
     }
     fclose(f);
-    // only a clean end of file ends the entries: a truncated or unparsable
-    // entry rejects the whole file, and nothing of it is merged
-    if (got != EOF) return set_error(HPXFFT_ERR_INVALID_ARG, "corrupt wisdom entry");
-    std::lock_guard<std::mutex> lock(g_cache_mu);
-    for (auto &r : rows) g_cache[r.first] = r.second;
+    int version = 0;
+    {
+        char head[64] = {};
+        if (lines.empty() || sscanf(lines[0].c_str(), "%63s %d", head, &version) != 2 ||
+            strcmp(head, "hpxfft-gb300-wisdom") || (version != 1 && version != 2))
+            return set_error(HPXFFT_ERR_INVALID_ARG, "not a wisdom file");
+    }
+    std::vector<std::pair<std::string, Tuning>> rows;
+    std::vector<std::pair<std::string, std::vector<long long>>> rows2d;
+    for (size_t i = 1; i < lines.size(); ++i) {
+        const std::string &ln = lines[i];
+        if (ln.find_first_not_of(" \t\r") == std::string::npos) continue;
+        const size_t sp = ln.find(' ');
+        if (sp == std::string::npos || sp == 0) return set_error(HPXFFT_ERR_INVALID_ARG, "corrupt wisdom entry");
+        const std::string key = ln.substr(0, sp);
+        std::vector<long long> v;
+        const char *q = ln.c_str() + sp;
+        for (;;) {
+            while (*q == ' ' || *q == '\t' || *q == '\r') ++q;
+            if (!*q) break;
+            char *end = nullptr;
+            const long long x = strtoll(q, &end, 10);
+            if (end == q) return set_error(HPXFFT_ERR_INVALID_ARG, "corrupt wisdom entry");
+            v.push_back(x);
+            q = end;
+        }
+        if (key.rfind("2d;", 0) == 0) {
+            if (version < 2 || !wisdom2d_check(key, v)) return set_error(HPXFFT_ERR_INVALID_ARG, "corrupt wisdom entry");
+            rows2d.push_back({key, v});
+            continue;
+        }
+        if (v.size() != 2 || v[0] < 0 || v[0] > 4096 || v[1] < 1 || v[1] > 8)
+            return set_error(HPXFFT_ERR_INVALID_ARG, "corrupt wisdom entry");
+        Tuning t;
+        t.lag = (int)v[0];
+        t.ctas_per_sm = (int)v[1];
+        rows.push_back({key, t});
+    }
+    {
+        std::lock_guard<std::mutex> lock(g_cache_mu);
+        for (auto &r : rows) g_cache[r.first] = r.second;
+    }
+    for (auto &r : rows2d) wisdom2d_add(r.first, r.second);
     return HPXFFT_OK;
 }
 
 int hpxfft_wisdom_forget(void)
 {
-    std::lock_guard<std::mutex> lock(g_cache_mu);
-    g_cache.clear();
+    {
+        std::lock_guard<std::mutex> lock(g_cache_mu);
+        g_cache.clear();
+    }
+    wisdom2d_forget();
     return HPXFFT_OK;
 }
 

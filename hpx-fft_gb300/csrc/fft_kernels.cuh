@@ -28,6 +28,31 @@ struct PassPlan {
     int radix[kMaxPasses];
 };
 
+// Radix sequence of a runtime-planned local length L: radix-16 passes, then
+// the power-of-two remainder, then the odd primes 3, 5, 7, 11, 13.  False
+// when L has a prime factor above 13 or needs more than kMaxPasses passes.
+// Uses no heap (the allocation-free entry point plans with it too).
+inline bool factorize_radices(int L, PassPlan &pp)
+{
+    pp.n = 0;
+    if (L < 1) return false;
+    int odd[kMaxPasses], nodd = 0, rest = L;
+    for (int q : {3, 5, 7, 11, 13})
+        while (rest % q == 0) {
+            if (nodd == kMaxPasses) return false;
+            rest /= q;
+            odd[nodd++] = q;
+        }
+    if (rest & (rest - 1)) return false;  // a prime factor above 13
+    int p2 = 0;
+    while ((1 << p2) < rest) ++p2;
+    if (p2 / 4 + (p2 % 4 ? 1 : 0) + nodd > kMaxPasses) return false;
+    for (; p2 >= 4; p2 -= 4) pp.radix[pp.n++] = 16;
+    if (p2 > 0) pp.radix[pp.n++] = 1 << p2;
+    for (int i = 0; i < nodd; ++i) pp.radix[pp.n++] = odd[i];
+    return true;
+}
+
 // Compute-type traits: T = arithmetic type, S = storage (HBM) real type.
 // kFixedChains: compile-time pass chains are instantiated for this type.
 // kEPTFixed: elements per thread of the compile-time chains (also their

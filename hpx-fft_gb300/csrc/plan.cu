@@ -10,6 +10,7 @@
 // page-locked memory), the 3D plans and the allocation-free entry point.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -39,6 +40,18 @@ static int cuda_fail(cudaError_t e, const char *what)
 {
     return fail(HPXFFT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
+
+// The plan's tunable choices; -1 leaves a choice to the fixed rules.
+//   columns     1: single-kernel (cluster) column pass, 2: two-kernel four-step pass
+//   ff_pairs    float-float forward: raw (hi, lo) pairs between the kernels (1) or doubles (0)
+//   tc_vectors  split-BF16 column steps: 256 or 512 length-16 vectors per CTA
+//   tc_rows     split-BF16: tensor-core rows (1) or FP32 rows (0)
+struct PlanChoice {
+    int columns = -1;
+    int ff_pairs = -1;
+    int tc_vectors = -1;
+    int tc_rows = -1;
+};
 
 struct DimPlan {
     LaunchShape shape{};
@@ -92,32 +105,14 @@ struct hpxfft_plan_s {
     double sum_first = 0, sum_second = 0, sum_total = 0, sum_step_a = 0;
     long long nsum = 0;
     std::map<std::string, double> meas;
+    hpxfft_gpu::PlanChoice choice;  // the choices in effect (resolved, no -1)
+    // plan search under "measure" and stronger flags: each distinct candidate
+    // and its best time (ms); empty for "estimate" and for a cached choice
+    std::vector<std::pair<std::string, double>> tuning;
+    std::string tuned_from;  // "rules", "search" or "wisdom"
 };
 
 namespace hpxfft_gpu {
-
-// radix sequence for a local length L: 16s first, then the power-of-two
-// remainder, then the odd primes 3, 5, 7, 11, 13
-static bool factorize(int L, int max_radix, PassPlan &pp)
-{
-    pp.n = 0;
-    int rest = L;
-    std::vector<int> odd;
-    for (int q : {3, 5, 7, 11, 13})
-        while (rest % q == 0) rest /= q, odd.push_back(q);
-    if (rest & (rest - 1)) return false;  // a prime factor above 13
-    int p2 = 0;
-    while ((1 << p2) < rest) ++p2;
-    const int lmax = max_radix == 16 ? 4 : 3;
-    std::vector<int> r;
-    while (p2 >= lmax) r.push_back(1 << lmax), p2 -= lmax;
-    if (p2 > 0) r.push_back(1 << p2);
-    for (int q : odd) r.push_back(q);
-    if ((int)r.size() > kMaxPasses) return false;
-    pp.n = (int)r.size();
-    for (size_t i = 0; i < r.size(); ++i) pp.radix[i] = r[i];
-    return true;
-}
 
 // Elements of one CTA's transform(s): 4096 float-float (or FP64) pairs or
 // 8192 FP32 pairs, 64 KB of data, so two CTAs share an SM.
@@ -150,7 +145,7 @@ static bool plan_rows(hpxfft_plan_s &p)
         if (C > 1 && L % C) continue;
         if (L > maxel) continue;
         PassPlan pp;
-        if (!factorize(L, 16, pp)) return false;
+        if (!factorize_radices(L, pp)) return false;
         int log2W = 0;
         if (C == 1)
             while (log2W < 4 && (L << (log2W + 1)) <= packel && ((size_t)1 << log2W) < p.nx) ++log2W;
@@ -185,7 +180,7 @@ static bool plan_cols(hpxfft_plan_s &p)
             if (C > 1 && L % C) continue;
             if ((L << log2W) > maxel) continue;
             PassPlan pp;
-            if (!factorize(L, 16, pp)) return false;
+            if (!factorize_radices(L, pp)) return false;
             DimPlan &d = p.col;
             d.C = C;
             d.L = L;
@@ -228,14 +223,12 @@ static bool plan_colsteps(hpxfft_plan_s &p)
     if (p.prec == HPXFFT_PREC_BF16X3) {
         // tensor-core steps: nv length-16 vectors per CTA, 16 nv / L columns;
         // 256 (four CTAs per SM) measured faster than 512 on 16384^2 (1.91 vs
-        // 2.18 ms); HPXFFT_TC_VECTORS=256|512 overrides (tuning, tests)
-        int nv = 256;
-        const char *env = std::getenv("HPXFFT_TC_VECTORS");
-        if (env && !strcmp(env, "512")) nv = 512;
+        // 2.18 ms) and is the rule; the plan's choice may set 512
+        const int nv = p.choice.tc_vectors == 512 ? 512 : 256;
         for (int step = 0; step < 2; ++step) {
             DimPlan &d = step == 0 ? p.colA : p.colB;
             const int L = step == 0 ? p.N2 : p.N1;
-            if (!TcColStepLaunch::supports(L) || !factorize(L, 16, d.pp)) return false;
+            if (!TcColStepLaunch::supports(L) || !factorize_radices(L, d.pp)) return false;
             d.C = 1;
             d.L = L;
             d.log2W = TcColStepLaunch::log2W(L, nv);
@@ -264,7 +257,7 @@ static bool plan_colsteps(hpxfft_plan_s &p)
         d.log2W = full;
         if (full > log2W && has_fixed_step(p.prec, d)) log2W = full;
         PassPlan pp;
-        if (!factorize(L, 16, pp)) return false;
+        if (!factorize_radices(L, pp)) return false;
         d.C = 1;
         d.L = L;
         d.log2W = log2W;
@@ -710,11 +703,44 @@ int hpxfft_plan_flag_valid(const char *plan_flag) { return valid_flag(plan_flag)
 
 }  // extern "C"
 
+namespace hpxfft_gpu {
+
+// Choices forced through the environment (tests and manual tuning):
+// HPXFFT_COLUMNS=cluster|steps, HPXFFT_FF_PAIRS=0|1, HPXFFT_TC_VECTORS=256|512,
+// HPXFFT_TC_ROWS=0|1.  They override the rules and the plan search, which
+// then varies only the other choices.
+static PlanChoice env_choice()
+{
+    PlanChoice c;
+    if (const char *v = std::getenv("HPXFFT_COLUMNS")) {
+        if (!strcmp(v, "cluster")) c.columns = 1;
+        if (!strcmp(v, "steps")) c.columns = 2;
+    }
+    if (const char *v = std::getenv("HPXFFT_FF_PAIRS")) c.ff_pairs = !strcmp(v, "0") ? 0 : 1;
+    if (const char *v = std::getenv("HPXFFT_TC_VECTORS")) c.tc_vectors = !strcmp(v, "512") ? 512 : 256;
+    if (const char *v = std::getenv("HPXFFT_TC_ROWS")) c.tc_rows = !strcmp(v, "0") ? 0 : 1;
+    return c;
+}
+
+static PlanChoice merged_choice(const PlanChoice &forced)
+{
+    PlanChoice c = forced;
+    const PlanChoice env = env_choice();
+    if (env.columns >= 0) c.columns = env.columns;
+    if (env.ff_pairs >= 0) c.ff_pairs = env.ff_pairs;
+    if (env.tc_vectors >= 0) c.tc_vectors = env.tc_vectors;
+    if (env.tc_rows >= 0) c.tc_rows = env.tc_rows;
+    return c;
+}
+
+}  // namespace hpxfft_gpu
+
 // columns_only: a plan of the column pass alone (c2c along n_row of n_col/2
 // complex columns), the last axis of a 3D transform; no row plan, no row
-// twiddles, no float-float pair exchange.
-static int create_plan(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batch, int precision,
-                       const char *plan_flag, bool columns_only)
+// twiddles, no float-float pair exchange.  `forced` sets the tunable
+// choices (-1: the rules); the environment overrides both.
+static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batch, int precision,
+                            const char *plan_flag, bool columns_only, const PlanChoice &forced)
 {
     if (!out) return fail(HPXFFT_ERR_INVALID_ARG, "plan pointer is null");
     *out = nullptr;
@@ -744,6 +770,8 @@ static int create_plan(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
     p->real_bytes = f32_storage(precision) ? 4 : 8;
     p->tw_elem = f32_storage(precision) ? 8 : 16;
     p->columns_only = columns_only;
+    const PlanChoice want = merged_choice(forced);
+    p->choice.tc_vectors = want.tc_vectors == 512 ? 512 : 256;
     if ((!columns_only && !plan_rows(*p)) || !plan_cols(*p)) {
         delete p;
         return fail(HPXFFT_ERR_UNSUPPORTED_SIZE,
@@ -778,12 +806,11 @@ static int create_plan(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
     int rc = columns_only ? HPXFFT_OK : setup_fixed(*p, p->row, true, p->stream);
     if (rc == HPXFFT_OK) rc = setup_fixed(*p, p->col, false, p->stream);
     // column strategy: the two-kernel pass streams 512-byte row segments and
-    // wins once the cluster kernel needs 8 or more CTAs per strip
-    // HPXFFT_COLUMNS=cluster|steps overrides the choice (tuning and tests)
-    const char *force = std::getenv("HPXFFT_COLUMNS");
+    // wins once the cluster kernel needs 8 or more CTAs per strip (the rule;
+    // the plan's choice may set either)
     bool want_steps = p->col.C >= 8;
-    if (force && !strcmp(force, "cluster")) want_steps = false;
-    if (force && !strcmp(force, "steps")) want_steps = true;
+    if (want.columns == 1) want_steps = false;
+    if (want.columns == 2) want_steps = true;
     if (precision == HPXFFT_PREC_BF16X3) {
         // the tensor-core stage lives in the column steps: nx = N1 * N2 with
         // N1, N2 in {32, 64, 128, 256}
@@ -805,13 +832,12 @@ static int create_plan(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
                 // rows: the tensor-core r2c where the FP32 plan has a compiled
                 // single-CTA shape of 128..512 vectors; other rows stay FP32
                 // (the launcher sizes its own CTAs; row.shape stays the FP32
-                // one, which the inverse's c2r rows use).  HPXFFT_TC_ROWS=0
-                // keeps FP32 rows (16384^2: 0.61 ms against 0.93 ms for the
-                // tensor-core row, whose BF16 split costs more CUDA-core
-                // work than the radix-16 butterfly it replaces)
-                const char *rows_env = std::getenv("HPXFFT_TC_ROWS");
+                // one, which the inverse's c2r rows use).  The choice
+                // tc_rows = 0 keeps FP32 rows (16384^2: 0.61 ms against
+                // 0.93 ms for the tensor-core row, whose BF16 split costs
+                // more CUDA-core work than the radix-16 butterfly it replaces)
                 if (!columns_only && p->row.FL && TcRowLaunch::supports((int)p->M, p->row.log2W, p->row.C) &&
-                    !(rows_env && !strcmp(rows_env, "0")))
+                    want.tc_rows != 0)
                     p->tc_rows = true;
             }
         }
@@ -829,10 +855,9 @@ static int create_plan(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
         }
     }
     // float-float pair exchange between the forward kernels (compiled step
-    // shapes only); HPXFFT_FF_PAIRS=0 keeps doubles in between (tests, tuning)
-    const char *pairs_env = std::getenv("HPXFFT_FF_PAIRS");
+    // shapes only); the choice ff_pairs = 0 keeps doubles in between
     if (rc == HPXFFT_OK && !columns_only && precision == HPXFFT_PREC_F64 && p->col_two_step && p->colA.FL && p->colB.FL &&
-        p->colA.L <= kColStepMaxPairL && p->colB.L <= kColStepMaxPairL && !(pairs_env && !strcmp(pairs_env, "0"))) {
+        p->colA.L <= kColStepMaxPairL && p->colB.L <= kColStepMaxPairL && want.ff_pairs != 0) {
         if (cudaMalloc(&p->exp_rows, sizeof(int) * p->nx * p->batch) != cudaSuccess ||
             cudaMalloc(&p->exp_step_a, sizeof(int) * p->colA.shape.grid.x * p->batch) != cudaSuccess) {
             cudaGetLastError();
@@ -868,9 +893,269 @@ static int create_plan(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
     const double f_r2c = 2.5 * ny * std::log2(ny), f_c2c = nx > 1 ? 5.0 * nx * std::log2(nx) : 0.0;
     p->meas["plan_flops"] = ny * f_r2c + nx * f_c2c;
     p->meas["plan_flops_actual"] = (nx * f_r2c + (double)p->dcy * f_c2c) * (double)batch;
+    // the choices in effect
+    p->choice.columns = p->col_two_step ? 2 : 1;
+    p->choice.ff_pairs = p->ff_pairs ? 1 : 0;
+    p->choice.tc_rows = p->tc_rows ? 1 : 0;
+    if (!p->tc_cols) p->choice.tc_vectors = 0;
+    p->tuned_from = "rules";
     *out = p;
     return HPXFFT_OK;
 }
+
+// ------------------------------------------------------------ plan search
+// "estimate" plans by the fixed rules.  "measure", "patient" and
+// "exhaustive" time every distinct candidate plan (column strategy,
+// float-float pair exchange, split-BF16 vectors per CTA and tensor-core
+// rows) on scratch arrays of the plan's size, keep the fastest and cache the
+// choice under (shape, batch, precision, device architecture); the cache is
+// written to and read from wisdom files with the batch plans'.  This is the
+// planner step of fftw_adapter::{r2c_1d,c2c_1d}::plan
+// (core/src/util/adapter_fftw.cpp:6-10,24-30) with FFTW_MEASURE and stronger
+// (core/include/hpxfft/util/adapter_fftw.hpp:13-44), which run trial
+// transforms on a scratch row (core/src/shared/loop.cpp:169-182).
+namespace hpxfft_gpu {
+
+// HPXFFT_ERR_TIMEOUT (and clears the flag) when a tensor-core kernel's wait gave up
+static int check_device_error(hpxfft_plan p)
+{
+    if (!p->dev_error) return HPXFFT_OK;
+    int flag = 0;
+    cudaError_t e = cudaMemcpyAsync(&flag, p->dev_error, sizeof(int), cudaMemcpyDeviceToHost, p->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "error flag");
+    if (!flag) return HPXFFT_OK;
+    cudaMemsetAsync(p->dev_error, 0, sizeof(int), p->stream);
+    return fail(HPXFFT_ERR_TIMEOUT, "tensor-core MMA completion wait timed out");
+}
+
+static std::mutex g_choice_mu;
+static std::map<std::string, PlanChoice> g_choices;
+
+static std::string choice_key(size_t n_row, size_t n_col, size_t batch, int prec, bool columns_only)
+{
+    int dev = 0, major = 0, minor = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) ||
+        cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev))
+        cudaGetLastError();
+    char buf[160];
+    snprintf(buf, sizeof(buf), "2d;p%d;%zux%zu;b%zu;%s;sm%d%d", prec, n_row, n_col, batch, columns_only ? "cols" : "full",
+             major, minor);
+    return buf;
+}
+
+std::string describe_choice(const PlanChoice &c)
+{
+    std::string d = c.columns == 2 ? "columns=steps" : "columns=cluster";
+    if (c.columns == 2) d += " ff_pairs=" + std::to_string(c.ff_pairs);
+    if (c.tc_vectors > 0) d += " tc_vectors=" + std::to_string(c.tc_vectors) + " tc_rows=" + std::to_string(c.tc_rows);
+    return d;
+}
+
+template <class S>
+__global__ void tune_fill_kernel(S *p, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        unsigned h = (unsigned)(i * 2654435761u) ^ (unsigned)(i >> 32) ^ 0x9e3779b9u;
+        h ^= h >> 16;
+        h *= 0x7feb352du;
+        h ^= h >> 15;
+        p[i] = (S)((float)(h >> 8) * (2.0f / 16777216.0f) - 1.0f);  // uniform[-1, 1)
+    }
+}
+
+// Best time (ms) of `reps` transforms of plan q from `in` to `out` after one warm-up.
+static double time_candidate(hpxfft_plan q, const void *in, void *out, int reps)
+{
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        cudaGetLastError();
+        if (e0) cudaEventDestroy(e0);
+        return -1.0;
+    }
+    double best = -1.0;
+    for (int r = 0; r <= reps; ++r) {
+        if (cudaMemcpyAsync(out, in, q->nx * q->ncol * q->real_bytes * q->batch, cudaMemcpyDeviceToDevice,
+                            q->stream) != cudaSuccess)
+            break;
+        cudaEventRecord(e0, q->stream);
+        cudaError_t e = q->columns_only ? dispatch_columns_only(*q, out) : dispatch_forward(*q, in, out);
+        cudaEventRecord(e1, q->stream);
+        if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+            best = -1.0;
+            break;
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r > 0 && (best < 0 || ms < best)) best = ms;
+    }
+    cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (collect(*q) != HPXFFT_OK || check_device_error(q) != HPXFFT_OK) return -1.0;
+    return best;
+}
+
+// Forget what the trial runs left in a plan's measurements and timing sums.
+static void clear_trial_state(hpxfft_plan q)
+{
+    collect(*q);
+    q->sum_first = q->sum_second = q->sum_total = q->sum_step_a = 0.0;
+    q->nsum = 0;
+    std::map<std::string, double> keep;
+    for (const char *k : {"plan", "plan_flops", "plan_flops_actual"}) keep[k] = q->meas[k];
+    q->meas.swap(keep);
+}
+
+}  // namespace hpxfft_gpu
+
+static int create_plan(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batch, int precision,
+                       const char *plan_flag, bool columns_only)
+{
+    if (!valid_flag(plan_flag) || !strcmp(plan_flag, "estimate"))
+        return create_plan_with(out, n_row, n_col, batch, precision, plan_flag, columns_only, PlanChoice{});
+    const auto t0 = std::chrono::steady_clock::now();
+    auto finish = [&](hpxfft_plan q, const char *from) {
+        q->flag = plan_flag;
+        q->tuned_from = from;
+        q->meas["plan"] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        q->meas["cached_plan"] = !strcmp(from, "wisdom") ? 1.0 : 0.0;
+        q->meas["autotune_candidates"] = (double)q->tuning.size();
+        q->meas["choice_columns"] = q->choice.columns;
+        q->meas["choice_ff_pairs"] = q->choice.ff_pairs;
+        q->meas["choice_tc_vectors"] = q->choice.tc_vectors;
+        q->meas["choice_tc_rows"] = q->choice.tc_rows;
+        *out = q;
+        return HPXFFT_OK;
+    };
+    const std::string key = choice_key(n_row, n_col, batch, precision, columns_only);
+    {
+        PlanChoice cached;
+        bool hit = false;
+        {
+            std::lock_guard<std::mutex> lock(g_choice_mu);
+            auto it = g_choices.find(key);
+            if (it != g_choices.end()) cached = it->second, hit = true;
+        }
+        if (hit) {
+            hpxfft_plan q = nullptr;
+            int rc = create_plan_with(&q, n_row, n_col, batch, precision, "estimate", columns_only, cached);
+            if (rc != HPXFFT_OK) return rc;
+            return finish(q, "wisdom");
+        }
+    }
+    // candidates: every combination of the choices this precision has, less
+    // those the environment fixes; plans that come out identical are timed once
+    const PlanChoice env = env_choice();
+    std::vector<int> cols = env.columns >= 0 ? std::vector<int>{env.columns} : std::vector<int>{2, 1};
+    std::vector<int> pairs{-1}, vecs{-1}, trows{-1};
+    if (precision == HPXFFT_PREC_F64 && env.ff_pairs < 0) pairs = {1, 0};
+    if (precision == HPXFFT_PREC_BF16X3) {
+        if (env.tc_vectors < 0) vecs = {256, 512};
+        if (env.tc_rows < 0) trows = {1, 0};
+    }
+    const int reps = !strcmp(plan_flag, "measure") ? 3 : !strcmp(plan_flag, "patient") ? 5 : 10;
+    std::vector<hpxfft_plan> plans;
+    std::vector<std::string> seen;
+    int first_rc = HPXFFT_OK;
+    std::string first_msg;
+    for (int c : cols)
+        for (int fp : pairs)
+            for (int nv : vecs)
+                for (int tr : trows) {
+                    PlanChoice cand;
+                    cand.columns = c;
+                    cand.ff_pairs = fp;
+                    cand.tc_vectors = nv;
+                    cand.tc_rows = tr;
+                    hpxfft_plan q = nullptr;
+                    int rc = create_plan_with(&q, n_row, n_col, batch, precision, "estimate", columns_only, cand);
+                    if (rc != HPXFFT_OK) {
+                        if (first_rc == HPXFFT_OK) first_rc = rc, first_msg = g_last_error;
+                        continue;
+                    }
+                    const std::string d = describe_choice(q->choice);
+                    if (std::find(seen.begin(), seen.end(), d) != seen.end()) {
+                        hpxfft_plan_destroy(q);
+                        continue;
+                    }
+                    seen.push_back(d);
+                    plans.push_back(q);
+                }
+    if (plans.empty()) return fail(first_rc == HPXFFT_OK ? HPXFFT_ERR_UNSUPPORTED_SIZE : first_rc, first_msg);
+    size_t best = 0;
+    std::vector<double> ms(plans.size(), -1.0);
+    if (plans.size() > 1) {
+        // trial arrays of the plan's size, filled with uniform[-1, 1) values
+        const size_t bytes = n_row * n_col * plans[0]->real_bytes * batch;
+        void *bin = nullptr, *bout = nullptr;
+        if (cudaMalloc(&bin, bytes) == cudaSuccess && cudaMalloc(&bout, bytes) == cudaSuccess) {
+            if (plans[0]->real_bytes == 8)
+                tune_fill_kernel<double><<<1024, 256, 0, plans[0]->stream>>>((double *)bin, bytes / 8);
+            else
+                tune_fill_kernel<float><<<1024, 256, 0, plans[0]->stream>>>((float *)bin, bytes / 4);
+            cudaStreamSynchronize(plans[0]->stream);
+            for (size_t i = 0; i < plans.size(); ++i) ms[i] = time_candidate(plans[i], bin, bout, reps);
+            for (size_t i = 0; i < plans.size(); ++i)
+                if (ms[i] >= 0 && (ms[best] < 0 || ms[i] < ms[best])) best = i;
+        }
+        cudaGetLastError();
+        cudaFree(bin);
+        cudaFree(bout);
+    }
+    for (size_t i = 0; i < plans.size(); ++i)
+        if (i != best) hpxfft_plan_destroy(plans[i]);
+    hpxfft_plan q = plans[best];
+    clear_trial_state(q);
+    if (plans.size() > 1 && ms[best] >= 0) {
+        for (size_t i = 0; i < seen.size(); ++i) q->tuning.push_back({seen[i], ms[i]});
+        q->meas["autotune_best_ms"] = ms[best];
+        q->meas["autotune_chosen"] = (double)best;
+        for (size_t i = 0; i < ms.size(); ++i) q->meas["autotune_ms_" + std::to_string(i)] = ms[i];
+    }
+    {
+        std::lock_guard<std::mutex> lock(g_choice_mu);
+        g_choices[key] = q->choice;
+    }
+    return finish(q, plans.size() > 1 ? "search" : "rules");
+}
+
+// wisdom of the 2D plans (the batch plans' entries are written by batch.cu)
+namespace hpxfft_gpu {
+
+void wisdom2d_write(FILE *f)
+{
+    std::lock_guard<std::mutex> lock(g_choice_mu);
+    for (auto &kv : g_choices)
+        fprintf(f, "%s %d %d %d %d\n", kv.first.c_str(), kv.second.columns, kv.second.ff_pairs, kv.second.tc_vectors,
+                kv.second.tc_rows);
+}
+
+// One entry "2d;... columns ff_pairs tc_vectors tc_rows"; false if malformed.
+bool wisdom2d_check(const std::string &key, const std::vector<long long> &v)
+{
+    return key.rfind("2d;", 0) == 0 && v.size() == 4 && (v[0] == 1 || v[0] == 2) && (v[1] == 0 || v[1] == 1) &&
+           (v[2] == 0 || v[2] == 256 || v[2] == 512) && (v[3] == 0 || v[3] == 1);
+}
+
+void wisdom2d_add(const std::string &key, const std::vector<long long> &v)
+{
+    PlanChoice c;
+    c.columns = (int)v[0];
+    c.ff_pairs = (int)v[1];
+    c.tc_vectors = (int)v[2];
+    c.tc_rows = (int)v[3];
+    std::lock_guard<std::mutex> lock(g_choice_mu);
+    g_choices[key] = c;
+}
+
+void wisdom2d_forget()
+{
+    std::lock_guard<std::mutex> lock(g_choice_mu);
+    g_choices.clear();
+}
+
+}  // namespace hpxfft_gpu
 
 extern "C" {
 
@@ -1049,18 +1334,6 @@ static int ensure_dbuf(hpxfft_plan p)
     return HPXFFT_OK;
 }
 
-// HPXFFT_ERR_TIMEOUT (and clears the flag) when a tensor-core kernel's wait gave up
-static int check_device_error(hpxfft_plan p)
-{
-    if (!p->dev_error) return HPXFFT_OK;
-    int flag = 0;
-    cudaError_t e = cudaMemcpyAsync(&flag, p->dev_error, sizeof(int), cudaMemcpyDeviceToHost, p->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
-    if (e != cudaSuccess) return cuda_fail(e, "error flag");
-    if (!flag) return HPXFFT_OK;
-    cudaMemsetAsync(p->dev_error, 0, sizeof(int), p->stream);
-    return fail(HPXFFT_ERR_TIMEOUT, "tensor-core MMA completion wait timed out");
-}
 
 // Device address of a page-locked (pinned or registered) host buffer, else null.
 static void *mapped_host(void *h)
@@ -1205,6 +1478,14 @@ int hpxfft_write_plan(hpxfft_plan p, const char *path)
     } else {
         fprintf(f, "GPU c2c 1D plan:\n%s\n\n", describe(*p, p->col, "c2c", p->nx).c_str());
     }
+    // how the plan's choices were made: fixed rules ("estimate"), a timed
+    // search over the candidates, or a cached (wisdom) choice
+    fprintf(f, "GPU plan choice (flag %s, from %s): %s\n", p->flag.c_str(), p->tuned_from.c_str(),
+            describe_choice(p->choice).c_str());
+    for (auto &c : p->tuning)
+        fprintf(f, "  candidate %s: %.4f ms%s\n", c.first.c_str(), c.second,
+                c.first == describe_choice(p->choice) ? " (chosen)" : "");
+    fprintf(f, "\n");
     fclose(f);
     return HPXFFT_OK;
 }
@@ -1249,66 +1530,11 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 static std::mutex g_noalloc_mutex;
 static void *g_noalloc_ptr[kMaxDevices];  // device address of g_noalloc_scratch, per device
 
-// factorize() without a heap allocation: the same radix rule into PassPlan
-static bool noalloc_factorize(int L, PassPlan &pp)
-{
-    int odd[kMaxPasses], nodd = 0, rest = L;
-    for (int q : {3, 5, 7, 11, 13})
-        while (rest % q == 0 && nodd < kMaxPasses) rest /= q, odd[nodd++] = q;
-    if (rest & (rest - 1)) return false;
-    int p2 = 0;
-    while ((1 << p2) < rest) ++p2;
-    pp.n = 0;
-    while (p2 >= 4 && pp.n < kMaxPasses) pp.radix[pp.n++] = 16, p2 -= 4;
-    if (p2 > 0 && pp.n < kMaxPasses) pp.radix[pp.n++] = 1 << p2;
-    for (int i = 0; i < nodd && pp.n < kMaxPasses; ++i) pp.radix[pp.n++] = odd[i];
-    return pp.n < kMaxPasses;
-}
-
-// The same shapes as plan_rows / plan_cols for the float-float type.
-static bool noalloc_shape(hpxfft_plan_s &p)
-{
-    const int maxel = max_elems_for(HPXFFT_PREC_F64);
-    for (int C : {1, 2, 4}) {
-        if (p.M % C) continue;
-        const int L = (int)(p.M / C);
-        if ((C > 1 && L % C) || L > maxel) continue;
-        if (!noalloc_factorize(L, p.row.pp)) return false;
-        int log2W = 0;
-        if (C == 1)
-            while (log2W < 4 && (L << (log2W + 1)) <= maxel && ((size_t)1 << log2W) < p.nx) ++log2W;
-        p.row.C = C;
-        p.row.L = L;
-        p.row.log2W = log2W;
-        const int nel = L << log2W;
-        p.row.shape.threads = threads_for(nel);
-        p.row.shape.smem = (size_t)padded_elems(nel) * 16;
-        p.row.shape.cluster = C;
-        p.row.shape.grid = dim3((unsigned)(((p.nx + ((size_t)1 << log2W) - 1) >> log2W) * C), 1, 1);
-        break;
-    }
-    if (p.row.L == 0) return false;
-    int pref = 2;
-    while (pref > 0 && ((size_t)1 << (pref - 1)) >= p.dcy) --pref;
-    for (int log2W = pref; log2W >= 0 && p.col.L == 0; --log2W) {
-        for (int C : {1, 2, 4, 8, 16}) {
-            if (p.nx % C) continue;
-            const int L = (int)(p.nx / C);
-            if ((C > 1 && L % C) || (L << log2W) > maxel) continue;
-            if (!noalloc_factorize(L, p.col.pp)) return false;
-            p.col.C = C;
-            p.col.L = L;
-            p.col.log2W = log2W;
-            const int nel = L << log2W;
-            p.col.shape.threads = threads_for(nel);
-            p.col.shape.smem = (size_t)padded_elems(nel) * 16;
-            p.col.shape.cluster = C;
-            p.col.shape.grid = dim3((unsigned)(((p.dcy + ((size_t)1 << log2W) - 1) >> log2W) * C), 1, 1);
-            break;
-        }
-    }
-    return p.col.L != 0;
-}
+// The plan's own row and column rules (plan_rows and plan_cols use no heap).
+// The columns always take the single-kernel cluster pass: the two-kernel
+// four-step pass a plan picks for power-of-two n_row >= 8192 needs a scratch
+// array as large as the data, which this entry point cannot allocate.
+static bool noalloc_shape(hpxfft_plan_s &p) { return plan_rows(p) && plan_cols(p); }
 
 // Per-pass tables of a compile-time chain written at `dst` (no allocation).
 static cudaError_t noalloc_fixed_tables(DimPlan &d, bool rows, unsigned char *dst, size_t cap, size_t &used,

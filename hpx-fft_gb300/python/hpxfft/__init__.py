@@ -16,4 +16,15 @@ from .plan import Plan, Plan3D
 from .batch import Batch
 from . import util, shared, distributed
 
-__all__ = ["Plan", "Plan3D", "Batch", "HpxFftError", "HpxFftInvalidArgument", "util", "shared", "distributed", "_capi"]
+__all__ = ["Plan", "Plan3D", "Batch", "HpxFftError", "HpxFftInvalidArgument", "util", "shared", "distributed", "_capi",
+           "pipe_peaks"]
+
+
+def pipe_peaks() -> dict:
+    """Measured FP32 and FP64 FMA throughput of the current device (TFLOP/s)."""
+    import ctypes
+
+    f32, f64 = ctypes.c_double(), ctypes.c_double()
+    _capi.check(_capi.load().hpxfft_measure_pipe_peaks(ctypes.byref(f32), ctypes.byref(f64)))
+    return {"fp32_fma_tflops": f32.value, "fp64_fma_tflops": f64.value,
+            "fp32_over_fp64": f32.value / f64.value if f64.value > 0 else None}

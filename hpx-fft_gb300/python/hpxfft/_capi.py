@@ -69,6 +69,7 @@ SIGNATURES = {
     "hpxfft_wisdom_export": (_ci, [_cs]),
     "hpxfft_wisdom_import": (_ci, [_cs]),
     "hpxfft_wisdom_forget": (_ci, []),
+    "hpxfft_measure_pipe_peaks": (_ci, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "hpxfft_host_alloc": (_ci, [ctypes.POINTER(_vp), _sz]),
     "hpxfft_host_free": (_ci, [_vp]),
 }

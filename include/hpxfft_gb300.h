@@ -62,10 +62,17 @@ typedef struct hpxfft_plan3d_s *hpxfft_plan3d;
 /* Plan a 2D r2c of `batch` equally sized arrays of n_row x n_col reals
  * (n_col = 2*(ny/2+1), so ny = n_col - 2).  plan_flag is one of
  * "estimate", "measure", "patient", "exhaustive"; anything else returns
- * HPXFFT_ERR_INVALID_ARG.  Every valid flag plans the same 2D transform (the
- * kernel, column strategy and launch shapes are fixed rules set by
- * measurements on GB300), so planning never runs trial transforms; the
- * batch plan is where "measure" and stronger flags time candidates.
+ * HPXFFT_ERR_INVALID_ARG.  "estimate" plans by fixed rules set by
+ * measurements on GB300.  "measure", "patient" and "exhaustive" run trial
+ * transforms of every distinct candidate plan (column strategy: cluster
+ * kernel or two-kernel four-step pass; float-float pair exchange between the
+ * kernels; split-BF16 vectors per CTA and tensor-core rows) on two scratch
+ * arrays of the plan's size (allocated and freed during the call), best of
+ * 3, 5 or 10 runs, and keep the fastest.  The choice is cached per shape,
+ * batch, precision and device architecture, so a later plan of the same kind
+ * runs no trials; hpxfft_wisdom_export / _import save and restore the cache.
+ * Measurements "cached_plan", "autotune_candidates", "autotune_ms_<i>",
+ * "autotune_best_ms" and "choice_*" describe the search.
  * Allocates the twiddle tables and no data buffer.
  * Sizes: ny even; ny/2 (the row's complex length) and n_row without a prime
  * factor above 13.  A row runs on a cluster of C in {1, 2, 4} CTAs of at
@@ -204,8 +211,9 @@ HPXFFT_API int hpxfft_batch_synchronize(hpxfft_batch batch);
  * "algorithmic_bytes", "cached_plan". */
 HPXFFT_API int hpxfft_batch_get_measurement(hpxfft_batch batch, const char *name, double *value);
 
-/* Tuned batch configurations, process-wide: write them to / read them from a
- * text file (the analogue of FFTW wisdom), or drop them. */
+/* Tuned plans, process-wide (batch queue configurations and 2D plan
+ * choices): write them to / read them from a text file (the analogue of
+ * FFTW wisdom), or drop them.  Import rejects a malformed file whole. */
 HPXFFT_API int hpxfft_wisdom_export(const char *path);
 HPXFFT_API int hpxfft_wisdom_import(const char *path);
 HPXFFT_API int hpxfft_wisdom_forget(void);
@@ -224,8 +232,24 @@ HPXFFT_API int hpxfft_wisdom_forget(void);
  * the GPU (other streams, other threads) race and must be serialised by the
  * caller.  The first call on a device does a one-time set-up (it looks up
  * the array's device address and sets kernel attributes); make that first
- * call before any stream capture.  No counterpart in the reference. */
+ * call before any stream capture.  "Allocates nothing" holds for this
+ * library's own calls: under CUDA's lazy module loading (the default) the
+ * driver loads the library's kernels on that first call and may reserve
+ * device memory for their code then.  Make the first call on each device
+ * before the caller's pool reserves its memory, or run with
+ * CUDA_MODULE_LOADING=EAGER.  Later calls, of any supported shape, load no
+ * further code.  Shapes whose lengths are not powers of two run kernels
+ * with per-thread local memory, for which the driver may enlarge its local
+ * memory reservation the first time such a shape runs.  The device-address
+ * cache has one slot per device index below 64.  No counterpart in the
+ * reference. */
 HPXFFT_API int hpxfft_execute_r2c_noalloc(const void *d_in, void *d_out, size_t n_row, size_t n_col, void *stream);
+
+/* Measured FP32 and FP64 FMA throughput of the current device, TFLOP/s
+ * (2 flops per FMA; about 40 ms of kernels, allocates a small buffer).  The
+ * FP64 drop-in's float-float arithmetic rests on the ratio of the two.  No
+ * reference counterpart. */
+HPXFFT_API int hpxfft_measure_pipe_peaks(double *fp32_tflops, double *fp64_tflops);
 
 /* Pinned host memory for fast host<->device copies (cudaHostAlloc). */
 HPXFFT_API int hpxfft_host_alloc(void **ptr, size_t bytes);

@@ -114,6 +114,35 @@ def test_measure_flag_tunes_and_wisdom_round_trip(gpu_lib, cuda, oracle_lib, tmp
         hb.wisdom_import(str(bad))
 
 
+def test_bounded_wait_runs_out_then_clean_run(gpu_lib, cuda, oracle_lib, monkeypatch):
+    """The column items' wait for their instance's rows is bounded.  With the
+    bound lowered to zero polls, a one-instance batch (1024 row items, then
+    its column items, 304 persistent CTAs) hands out its first column items
+    while row items are still in flight: those items give up at once, the
+    kernel skips them and returns, and synchronize reports
+    HPXFFT_ERR_TIMEOUT.  A batch planned afterwards with the default bound
+    transforms the same input correctly."""
+    shapes = [(4096, 4096)]
+    nr, nc = [4096], [4098]
+    monkeypatch.setenv("HPXFFT_BATCH_SPIN_LIMIT", "0")
+    with gpu_lib.Batch(nr, nc, "f32", "estimate") as b:
+        arena = fill_arena(cuda, b, shapes, 9)
+        x_host = arena.cpu().numpy().view(np.uint8).copy()
+        b.set_stream(cuda.cuda.current_stream().cuda_stream)
+        b.execute(arena.data_ptr())
+        with pytest.raises(gpu_lib.HpxFftError) as e:
+            b.synchronize()
+        assert e.value.status == gpu_lib._capi.HPXFFT_ERR_TIMEOUT
+        cuda.cuda.synchronize()  # the context is still usable
+    monkeypatch.delenv("HPXFFT_BATCH_SPIN_LIMIT")
+    with gpu_lib.Batch(nr, nc, "f32", "estimate") as b:
+        arena = cuda.from_numpy(x_host.view(np.float32).copy()).cuda()
+        run_batch(cuda, b, arena)
+        y = b.views(arena.cpu().numpy().view(np.uint8))[0]
+        x = b.views(x_host)[0]
+        assert rel_l2(y.view(np.complex64), oracle_spectrum(oracle_lib, x[:, :4096])) <= 2e-6
+
+
 def test_batch_argument_errors(gpu_lib, cuda):
     with pytest.raises(gpu_lib.HpxFftInvalidArgument):
         gpu_lib.Batch([8], [10], "f32", "fast")

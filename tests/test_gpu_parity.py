@@ -132,6 +132,20 @@ def test_16384_squared_fp64_vs_oracle(gpu_lib, cuda, oracle_lib):
     assert err <= 1e-12, err
 
 
+def test_16384_squared_fp32_vs_fp64_oracle(gpu_lib, cuda, oracle_lib):
+    """The precision configuration's FP32 path at 16384^2, uniform[-1,1)
+    input, against the FP64 oracle of the same (float-representable) input:
+    relative L2 <= 2e-6, and the max-abs error stays a small multiple of
+    float rounding at the largest |X|."""
+    x = np.random.default_rng(3).uniform(-1, 1, (16384, 16384)).astype(np.float32)
+    got = forward(gpu_lib, cuda, x, "f32")
+    ref = oracle_fwd(oracle_lib, x.astype(np.float64))
+    err = rel_l2(got, ref)
+    assert err <= 2e-6, err
+    max_abs = float(np.max(np.abs(got.astype(np.complex128) - ref)))
+    assert max_abs <= 64 * np.finfo(np.float32).eps * float(np.max(np.abs(ref))), max_abs
+
+
 def test_ramp_closed_form_large(gpu_lib, cuda):
     """Ramp x[i][j] = j at 8192 x 16384: known answer without an oracle run."""
     nx, ny = 8192, 16384

@@ -182,18 +182,22 @@ def test_distributed_comm_flag_is_validated(gpu_lib):
 
 
 def test_wisdom_file_round_trip_and_corrupt_files(gpu_lib, tmp_path):
-    """The tuned-plan cache file (host only): import then export gives the
-    same entries, sorted by key; a corrupt file is rejected whole and
+    """The tuned-plan cache file (host only): batch entries and 2D plan
+    choices; import then export gives the same entries, sorted by key; a
+    corrupt file is rejected whole and
     merges nothing; unopenable paths raise the I/O status, like
     loop::write_plans_to_file's std::runtime_error (core/src/shared/loop.cpp:197-201)."""
     from hpxfft import batch as hb
 
     capi = gpu_lib._capi
-    head = "hpxfft-gb300-wisdom 1\n"
-    entries = ["p2;512x642*3 16 3", "p2;256x514*8;384x258*8 8 2", "p0;64x66*1 0 1"]
+    head = "hpxfft-gb300-wisdom 2\n"
+    batch_entries = ["p2;512x642*3 16 3", "p2;256x514*8;384x258*8 8 2", "p0;64x66*1 0 1"]
+    # 2D plan choices: columns (1 cluster, 2 steps), ff_pairs, tc_vectors, tc_rows
+    plan_entries = ["2d;p0;16384x16386;b1;full;sm103 2 1 0 0", "2d;p3;4096x4098;b1;full;sm103 2 0 512 1"]
     good = tmp_path / "good.txt"
-    good.write_text(head + "\n".join(entries) + "\n")
+    good.write_text(head + "\n".join(batch_entries + plan_entries) + "\n")
     out = tmp_path / "out.txt"
+    expected = sorted(batch_entries) + sorted(plan_entries)
 
     def exported():
         hb.wisdom_export(str(out))
@@ -205,10 +209,19 @@ def test_wisdom_file_round_trip_and_corrupt_files(gpu_lib, tmp_path):
     try:
         assert exported() == []
         hb.wisdom_import(str(good))
-        assert exported() == sorted(entries)
+        assert exported() == expected
+        # a version-1 file (batch entries only) still imports
+        v1 = tmp_path / "v1.txt"
+        v1.write_text("hpxfft-gb300-wisdom 1\n" + batch_entries[0] + "\n")
+        hb.wisdom_import(str(v1))
+        assert exported() == expected
         corrupt = {
             "header": "not wisdom\n",
-            "version": "hpxfft-gb300-wisdom 2\n",
+            "version": "hpxfft-gb300-wisdom 3\n",
+            "2d entry in a version-1 file": "hpxfft-gb300-wisdom 1\n" + plan_entries[0] + "\n",
+            "2d columns": head + "2d;p0;8x10;b1;full;sm103 3 1 0 0\n",
+            "2d vectors": head + "2d;p3;8x10;b1;full;sm103 2 1 128 1\n",
+            "2d too few": head + "2d;p0;8x10;b1;full;sm103 2 1 0\n",
             "lag range": head + "k 5000 2\n",
             "negative lag": head + "k -1 2\n",
             "ctas low": head + "k 8 0\n",
@@ -222,11 +235,11 @@ def test_wisdom_file_round_trip_and_corrupt_files(gpu_lib, tmp_path):
             bad.write_text(text)
             with pytest.raises(gpu_lib.HpxFftInvalidArgument):
                 hb.wisdom_import(str(bad))
-            assert exported() == sorted(entries), name
+            assert exported() == expected, name
         empty = tmp_path / "empty.txt"
         empty.write_text(head)
         hb.wisdom_import(str(empty))
-        assert exported() == sorted(entries)
+        assert exported() == expected
         for call in (lambda: hb.wisdom_import(str(tmp_path / "missing.txt")),
                      lambda: hb.wisdom_export(str(tmp_path))):
             with pytest.raises(gpu_lib.HpxFftError) as e:

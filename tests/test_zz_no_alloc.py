@@ -86,3 +86,29 @@ def test_no_alloc_rejects_sizes_beyond_its_scratch(gpu_lib, cuda):
         rc = lib.hpxfft_execute_r2c_noalloc(p, p, n_row, n_col, None)
         assert rc == gpu_lib._capi.HPXFFT_ERR_UNSUPPORTED_SIZE
         assert b"16384" in lib.hpxfft_last_error()
+
+
+def test_no_alloc_leaves_device_memory_untouched_after_first_call(gpu_lib, cuda):
+    """After the first call on the device (the set-up call, which may load
+    code), a call of another shape changes the device's free memory by
+    nothing: the entry point allocates no device memory.  Both shapes have
+    power-of-two lengths, whose kernels use no per-thread local memory.
+    Inputs and outputs are allocated before the free memory is read."""
+    lib = gpu_lib._capi.load()
+    first = _padded_input(cuda, 1024, 2048, 11)
+    second = _padded_input(cuda, 2048, 512, 12)
+    out_first, out_second = cuda.empty_like(first), cuda.empty_like(second)
+    stream = ctypes.c_void_p(cuda.cuda.current_stream().cuda_stream)
+
+    def call(x, out):
+        rc = lib.hpxfft_execute_r2c_noalloc(ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                            x.shape[0], x.shape[1], stream)
+        assert rc == 0, lib.hpxfft_last_error().decode()
+        cuda.cuda.synchronize()
+
+    call(first, out_first)
+    free_before, _ = cuda.cuda.mem_get_info()
+    call(second, out_second)
+    free_after, _ = cuda.cuda.mem_get_info()
+    assert free_after == free_before, (free_before, free_after)
+    assert _rel_l2(out_second, _with_plan(gpu_lib, cuda, second)) <= 1e-12
