@@ -28,6 +28,8 @@ namespace hpxfft_gpu {
 
 static thread_local std::string g_last_error;
 constexpr int kMaxDevices = 64;
+// what a plan transforms: both passes, the column pass alone, the row pass alone
+constexpr int kPlanFull = 0, kPlanColumns = 1, kPlanRows = 2;
 
 static int fail(int status, const std::string &msg)
 {
@@ -101,6 +103,7 @@ struct hpxfft_plan_s {
     bool pending_copy = false;
     bool last_zero_copy = false;  // the last host-buffer transform read and wrote host memory directly
     bool columns_only = false;    // the column pass alone (the first axis of a 3D transform)
+    bool rows_only = false;       // the row pass alone (the local rows of a slab decomposition)
     double peak_gbps = 0.0;       // nominal DRAM bandwidth of the device (memory clock x bus width)
     double sum_first = 0, sum_second = 0, sum_total = 0, sum_step_a = 0;
     long long nsum = 0;
@@ -585,6 +588,32 @@ static cudaError_t run_columns_only(hpxfft_plan_s &p, void *data)
     return cudaSuccess;
 }
 
+// The row pass alone, forward, `in` to `out` (timed like a transform: the
+// column slot of the timing ring is empty).  Doubles in and out for FP64.
+template <class A>
+static cudaError_t run_rows_only(hpxfft_plan_s &p, const void *in, void *out)
+{
+    cudaError_t e;
+    cudaEvent_t *ev = next_slot(p);
+    if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
+    RowArgs ra = row_args(p, in, out, 0);
+    ra.prefetch = 1;
+    if ((e = RowLaunch<A>::r2c(ra, p.row.shape, p.row.FL, p.stream)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(ev[2], p.stream)) != cudaSuccess) return e;
+    ++p.next;
+    return cudaSuccess;
+}
+
+static cudaError_t dispatch_rows_only(hpxfft_plan_s &p, const void *in, void *out)
+{
+    switch (p.prec) {
+    case HPXFFT_PREC_F64: return run_rows_only<ArithFF>(p, in, out);
+    case HPXFFT_PREC_F64_NATIVE: return run_rows_only<ArithF64>(p, in, out);
+    default: return run_rows_only<ArithF32>(p, in, out);
+    }
+}
+
 static cudaError_t dispatch_columns_only(hpxfft_plan_s &p, void *data)
 {
     switch (p.prec) {
@@ -735,13 +764,16 @@ static PlanChoice merged_choice(const PlanChoice &forced)
 
 }  // namespace hpxfft_gpu
 
-// columns_only: a plan of the column pass alone (c2c along n_row of n_col/2
-// complex columns), the last axis of a 3D transform; no row plan, no row
-// twiddles, no float-float pair exchange.  `forced` sets the tunable
-// choices (-1: the rules); the environment overrides both.
+// mode kPlanColumns: a plan of the column pass alone (c2c along n_row of
+// n_col/2 complex columns), the last axis of a 3D transform or the column
+// slab of a slab decomposition; no row plan, no row twiddles, no
+// float-float pair exchange.  kPlanRows: the row pass alone (FP32 rows for
+// split-BF16), the local rows of a slab decomposition.  `forced` sets the
+// tunable choices (-1: the rules); the environment overrides both.
 static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batch, int precision,
-                            const char *plan_flag, bool columns_only, const PlanChoice &forced)
+                            const char *plan_flag, int mode, const PlanChoice &forced)
 {
+    const bool columns_only = mode == kPlanColumns, rows_only = mode == kPlanRows;
     if (!out) return fail(HPXFFT_ERR_INVALID_ARG, "plan pointer is null");
     *out = nullptr;
     if (!valid_flag(plan_flag)) return fail(HPXFFT_ERR_INVALID_ARG, "Invalid FFTW plan flag string");
@@ -754,7 +786,7 @@ static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t
     // the split-BF16 column steps need nx = N1 * N2 with N1, N2 in
     // {32, 64, 128, 256}: the same condition plan_colsteps applies below,
     // checked here before anything touches the device
-    if (precision == HPXFFT_PREC_BF16X3 && (n_row < 1024 || n_row > 65536 || (n_row & (n_row - 1))))
+    if (precision == HPXFFT_PREC_BF16X3 && !rows_only && (n_row < 1024 || n_row > 65536 || (n_row & (n_row - 1))))
         return fail(HPXFFT_ERR_UNSUPPORTED_SIZE, "split-BF16 precision needs n_row a power of two in [1024, 65536]");
     const auto t0 = std::chrono::steady_clock::now();
     hpxfft_plan_s *p = new (std::nothrow) hpxfft_plan_s();
@@ -770,9 +802,10 @@ static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t
     p->real_bytes = f32_storage(precision) ? 4 : 8;
     p->tw_elem = f32_storage(precision) ? 8 : 16;
     p->columns_only = columns_only;
+    p->rows_only = rows_only;
     const PlanChoice want = merged_choice(forced);
     p->choice.tc_vectors = want.tc_vectors == 512 ? 512 : 256;
-    if ((!columns_only && !plan_rows(*p)) || !plan_cols(*p)) {
+    if ((!columns_only && !plan_rows(*p)) || (!rows_only && !plan_cols(*p))) {
         delete p;
         return fail(HPXFFT_ERR_UNSUPPORTED_SIZE,
                     "sizes must have no prime factor above 13 and fit the per-cluster shared memory");
@@ -799,19 +832,20 @@ static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t
             return cuda_fail(e, "event");
         }
     if ((!columns_only && cudaMalloc(&p->tw_row, p->tw_elem * 2 * p->M) != cudaSuccess) ||
-        cudaMalloc(&p->tw_col, p->tw_elem * p->nx) != cudaSuccess) {
+        (!rows_only && cudaMalloc(&p->tw_col, p->tw_elem * p->nx) != cudaSuccess)) {
         hpxfft_plan_destroy(p);
         return fail(HPXFFT_ERR_ALLOC, "twiddle tables");
     }
     int rc = columns_only ? HPXFFT_OK : setup_fixed(*p, p->row, true, p->stream);
-    if (rc == HPXFFT_OK) rc = setup_fixed(*p, p->col, false, p->stream);
+    if (rc == HPXFFT_OK && !rows_only) rc = setup_fixed(*p, p->col, false, p->stream);
     // column strategy: the two-kernel pass streams 512-byte row segments and
     // wins once the cluster kernel needs 8 or more CTAs per strip (the rule;
     // the plan's choice may set either)
     bool want_steps = p->col.C >= 8;
     if (want.columns == 1) want_steps = false;
     if (want.columns == 2) want_steps = true;
-    if (precision == HPXFFT_PREC_BF16X3) {
+    if (rows_only) want_steps = false;
+    if (precision == HPXFFT_PREC_BF16X3 && !rows_only) {
         // the tensor-core stage lives in the column steps: nx = N1 * N2 with
         // N1, N2 in {32, 64, 128, 256}
         if (rc == HPXFFT_OK && !plan_colsteps(*p)) {
@@ -872,7 +906,7 @@ static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t
         return fail(rc, msg);
     }
     if ((!columns_only && (e = gen_twiddles(precision, p->tw_row, (int)(2 * p->M), p->stream)) != cudaSuccess) ||
-        (e = gen_twiddles(precision, p->tw_col, (int)p->nx, p->stream)) != cudaSuccess ||
+        (!rows_only && (e = gen_twiddles(precision, p->tw_col, (int)p->nx, p->stream)) != cudaSuccess) ||
         (e = cudaStreamSynchronize(p->stream)) != cudaSuccess) {
         hpxfft_plan_destroy(p);
         return cuda_fail(e, "twiddle generation");
@@ -932,14 +966,15 @@ static int check_device_error(hpxfft_plan p)
 static std::mutex g_choice_mu;
 static std::map<std::string, PlanChoice> g_choices;
 
-static std::string choice_key(size_t n_row, size_t n_col, size_t batch, int prec, bool columns_only)
+static std::string choice_key(size_t n_row, size_t n_col, size_t batch, int prec, int mode)
 {
     int dev = 0, major = 0, minor = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) ||
         cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev))
         cudaGetLastError();
     char buf[160];
-    snprintf(buf, sizeof(buf), "2d;p%d;%zux%zu;b%zu;%s;sm%d%d", prec, n_row, n_col, batch, columns_only ? "cols" : "full",
+    snprintf(buf, sizeof(buf), "2d;p%d;%zux%zu;b%zu;%s;sm%d%d", prec, n_row, n_col, batch,
+             mode == kPlanColumns ? "cols" : mode == kPlanRows ? "rows" : "full",
              major, minor);
     return buf;
 }
@@ -979,7 +1014,9 @@ static double time_candidate(hpxfft_plan q, const void *in, void *out, int reps)
                             q->stream) != cudaSuccess)
             break;
         cudaEventRecord(e0, q->stream);
-        cudaError_t e = q->columns_only ? dispatch_columns_only(*q, out) : dispatch_forward(*q, in, out);
+        cudaError_t e = q->columns_only ? dispatch_columns_only(*q, out)
+                        : q->rows_only  ? dispatch_rows_only(*q, in, out)
+                                        : dispatch_forward(*q, in, out);
         cudaEventRecord(e1, q->stream);
         if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
             best = -1.0;
@@ -1010,10 +1047,10 @@ static void clear_trial_state(hpxfft_plan q)
 }  // namespace hpxfft_gpu
 
 static int create_plan(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batch, int precision,
-                       const char *plan_flag, bool columns_only)
+                       const char *plan_flag, int mode)
 {
     if (!valid_flag(plan_flag) || !strcmp(plan_flag, "estimate"))
-        return create_plan_with(out, n_row, n_col, batch, precision, plan_flag, columns_only, PlanChoice{});
+        return create_plan_with(out, n_row, n_col, batch, precision, plan_flag, mode, PlanChoice{});
     const auto t0 = std::chrono::steady_clock::now();
     auto finish = [&](hpxfft_plan q, const char *from) {
         q->flag = plan_flag;
@@ -1028,7 +1065,7 @@ static int create_plan(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
         *out = q;
         return HPXFFT_OK;
     };
-    const std::string key = choice_key(n_row, n_col, batch, precision, columns_only);
+    const std::string key = choice_key(n_row, n_col, batch, precision, mode);
     {
         PlanChoice cached;
         bool hit = false;
@@ -1039,7 +1076,7 @@ static int create_plan(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
         }
         if (hit) {
             hpxfft_plan q = nullptr;
-            int rc = create_plan_with(&q, n_row, n_col, batch, precision, "estimate", columns_only, cached);
+            int rc = create_plan_with(&q, n_row, n_col, batch, precision, "estimate", mode, cached);
             if (rc != HPXFFT_OK) return rc;
             return finish(q, "wisdom");
         }
@@ -1069,7 +1106,7 @@ static int create_plan(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batc
                     cand.tc_vectors = nv;
                     cand.tc_rows = tr;
                     hpxfft_plan q = nullptr;
-                    int rc = create_plan_with(&q, n_row, n_col, batch, precision, "estimate", columns_only, cand);
+                    int rc = create_plan_with(&q, n_row, n_col, batch, precision, "estimate", mode, cand);
                     if (rc != HPXFFT_OK) {
                         if (first_rc == HPXFFT_OK) first_rc = rc, first_msg = g_last_error;
                         continue;
@@ -1162,7 +1199,7 @@ extern "C" {
 int hpxfft_plan_create(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batch, int precision,
                        const char *plan_flag)
 {
-    return create_plan(out, n_row, n_col, batch, precision, plan_flag, false);
+    return create_plan(out, n_row, n_col, batch, precision, plan_flag, kPlanFull);
 }
 
 // ------------------------------------------------------------------ 3D r2c
@@ -1190,8 +1227,8 @@ int hpxfft_plan3d_create(hpxfft_plan3d *out, size_t n0, size_t n1, size_t n_col,
     p->n1 = n1;
     p->ncol = n_col;
     p->batch = batch;
-    int rc = create_plan(&p->slabs, n1, n_col, n0 * batch, precision, plan_flag, false);
-    if (rc == HPXFFT_OK) rc = create_plan(&p->axis0, n0, n1 * n_col, batch, precision, plan_flag, true);
+    int rc = create_plan(&p->slabs, n1, n_col, n0 * batch, precision, plan_flag, kPlanFull);
+    if (rc == HPXFFT_OK) rc = create_plan(&p->axis0, n0, n1 * n_col, batch, precision, plan_flag, kPlanColumns);
     if (rc != HPXFFT_OK) {
         std::string msg = g_last_error;
         hpxfft_plan3d_destroy(p);
@@ -1632,3 +1669,246 @@ extern "C" int hpxfft_execute_r2c_noalloc(const void *d_in, void *d_out, size_t 
         return cuda_fail(e, "column kernel");
     return HPXFFT_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Slab decomposition over P ranks (hpxfft_slab_*): the per-locality compute of
+// hpxfft::distributed::loop::fft_2d_r2c (core/src/distributed/loop.cpp:130-272)
+// with index maps that are correct for any P.  Rank r holds global rows
+// r * n_x_local + x of the padded input.  dcy = n_col / 2 complex columns are
+// split into P tiles of w = ceil(dcy / P) columns (the last tile padded with
+// zeros), so dcy need not be a multiple of P.
+//   rows:    row r2c of the local slab, then pack: send[d][x][k] = X[x][d w + k]
+//   (caller: all_to_all, tile d to rank d)
+//   columns: recv[s][x][k] is global row s n_x_local + x of my w columns, so
+//            recv is the column slab [nx][w]; column c2c in place; tile d of
+//            the result holds the rows kx of rank d: ready to send back
+//   (caller: all_to_all, tile d to rank d)
+//   finish:  out[x][s w + k] = recv2[s][x][k] for s w + k < dcy
+// The reference's transposes interleave the slabs cyclically, which is only
+// right for P = 1 (core/src/distributed/loop.cpp:87-127); its pack and
+// exchange steps are core/src/distributed/loop.cpp:19-84.
+// ---------------------------------------------------------------------------
+namespace hpxfft_gpu {
+
+template <class C>
+__global__ void slab_pack_kernel(const C *__restrict__ rows, C *__restrict__ send, int n_x_local, int dcy, int w)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x, d = blockIdx.z;
+    if (k >= w) return;
+    const int col = d * w + k;
+    for (int x = blockIdx.y; x < n_x_local; x += gridDim.y) {
+        C v{};
+        if (col < dcy) v = rows[(long long)x * dcy + col];
+        send[((long long)d * n_x_local + x) * w + k] = v;
+    }
+}
+
+template <class C>
+__global__ void slab_unpack_kernel(const C *__restrict__ recv, C *__restrict__ rows, int n_x_local, int dcy, int w)
+{
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= dcy) return;
+    const int s = col / w, k = col - s * w;
+    for (int x = blockIdx.y; x < n_x_local; x += gridDim.y)
+        rows[(long long)x * dcy + col] = recv[((long long)s * n_x_local + x) * w + k];
+}
+
+}  // namespace hpxfft_gpu
+
+struct hpxfft_slab_s {
+    hpxfft_plan rows = nullptr, cols = nullptr;
+    size_t nxl = 0, nx = 0, ncol = 0, dcy = 0, P = 1, rank = 0, w = 0, elem = 16;
+    int prec = HPXFFT_PREC_F64;
+    cudaEvent_t ev[8] = {};
+    bool ran_rows = false, ran_cols = false, ran_finish = false;
+    std::map<std::string, double> meas;
+};
+
+namespace hpxfft_gpu {
+
+static cudaError_t slab_pack(hpxfft_slab_s &s, const void *rows, void *send, cudaStream_t st)
+{
+    const unsigned gy = (unsigned)std::min<size_t>(s.nxl, 65535);
+    dim3 grid((unsigned)((s.w + 255) / 256), gy, (unsigned)s.P);
+    if (s.elem == 16)
+        slab_pack_kernel<double2><<<grid, 256, 0, st>>>((const double2 *)rows, (double2 *)send, (int)s.nxl,
+                                                         (int)s.dcy, (int)s.w);
+    else
+        slab_pack_kernel<float2><<<grid, 256, 0, st>>>((const float2 *)rows, (float2 *)send, (int)s.nxl, (int)s.dcy,
+                                                        (int)s.w);
+    return cudaGetLastError();
+}
+
+static cudaError_t slab_unpack(hpxfft_slab_s &s, const void *recv, void *rows, cudaStream_t st)
+{
+    const unsigned gy = (unsigned)std::min<size_t>(s.nxl, 65535);
+    dim3 grid((unsigned)((s.dcy + 255) / 256), gy, 1);
+    if (s.elem == 16)
+        slab_unpack_kernel<double2><<<grid, 256, 0, st>>>((const double2 *)recv, (double2 *)rows, (int)s.nxl,
+                                                           (int)s.dcy, (int)s.w);
+    else
+        slab_unpack_kernel<float2><<<grid, 256, 0, st>>>((const float2 *)recv, (float2 *)rows, (int)s.nxl,
+                                                          (int)s.dcy, (int)s.w);
+    return cudaGetLastError();
+}
+
+static double event_s(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+        cudaGetLastError();
+        return 0.0;
+    }
+    return 1e-3 * ms;
+}
+
+}  // namespace hpxfft_gpu
+
+extern "C" {
+
+int hpxfft_slab_create(hpxfft_slab *out, size_t n_row_local, size_t n_col, size_t n_ranks, size_t rank, int precision,
+                       const char *plan_flag)
+{
+    if (!out) return fail(HPXFFT_ERR_INVALID_ARG, "slab pointer is null");
+    *out = nullptr;
+    if (!valid_flag(plan_flag)) return fail(HPXFFT_ERR_INVALID_ARG, "Invalid FFTW plan flag string");
+    if (n_ranks == 0 || rank >= n_ranks) return fail(HPXFFT_ERR_INVALID_ARG, "rank must be below n_ranks");
+    if (n_row_local == 0) return fail(HPXFFT_ERR_INVALID_ARG, "empty slab");
+    if (n_col < 4 || n_col % 2) return fail(HPXFFT_ERR_UNSUPPORTED_SIZE, "n_col must be 2*(ny/2+1) with ny >= 2 even");
+    if (n_ranks > 65535 || n_row_local * n_ranks > (1u << 30))
+        return fail(HPXFFT_ERR_UNSUPPORTED_SIZE, "dimension too large");
+    hpxfft_slab_s *s = new (std::nothrow) hpxfft_slab_s();
+    if (!s) return fail(HPXFFT_ERR_ALLOC, "host allocation failed");
+    s->nxl = n_row_local;
+    s->P = n_ranks;
+    s->rank = rank;
+    s->nx = n_row_local * n_ranks;
+    s->ncol = n_col;
+    s->dcy = n_col / 2;
+    s->w = (s->dcy + n_ranks - 1) / n_ranks;
+    s->prec = precision;
+    s->elem = f32_storage(precision) ? 8 : 16;
+    int rc = create_plan(&s->rows, n_row_local, n_col, 1, precision, plan_flag, kPlanRows);
+    if (rc == HPXFFT_OK) rc = create_plan(&s->cols, s->nx, 2 * s->w, 1, precision, plan_flag, kPlanColumns);
+    for (auto &ev : s->ev)
+        if (rc == HPXFFT_OK && cudaEventCreate(&ev) != cudaSuccess) rc = fail(HPXFFT_ERR_CUDA, "event");
+    if (rc != HPXFFT_OK) {
+        std::string msg = g_last_error;
+        hpxfft_slab_destroy(s);
+        return fail(rc, msg);
+    }
+    s->cols->stream = s->rows->stream;  // one stream orders every phase
+    s->meas["plan"] = s->rows->meas["plan"] + s->cols->meas["plan"];
+    *out = s;
+    return HPXFFT_OK;
+}
+
+int hpxfft_slab_destroy(hpxfft_slab s)
+{
+    if (!s) return fail(HPXFFT_ERR_STATE, "null slab");
+    if (s->cols) {
+        if (s->rows) s->cols->stream = s->cols->own_stream;
+        hpxfft_plan_destroy(s->cols);
+    }
+    if (s->rows) hpxfft_plan_destroy(s->rows);
+    for (auto &ev : s->ev)
+        if (ev) cudaEventDestroy(ev);
+    delete s;
+    return HPXFFT_OK;
+}
+
+int hpxfft_slab_set_stream(hpxfft_slab s, void *stream)
+{
+    if (!s) return fail(HPXFFT_ERR_STATE, "null slab");
+    s->rows->stream = (cudaStream_t)stream;
+    s->cols->stream = (cudaStream_t)stream;
+    return HPXFFT_OK;
+}
+
+int hpxfft_slab_tile_bytes(hpxfft_slab s, size_t *bytes)
+{
+    if (!s || !bytes) return fail(HPXFFT_ERR_INVALID_ARG, "null argument");
+    *bytes = s->nxl * s->w * s->elem;
+    return HPXFFT_OK;
+}
+
+int hpxfft_slab_rows(hpxfft_slab s, void *d_values, void *d_send)
+{
+    if (!s) return fail(HPXFFT_ERR_STATE, "null slab");
+    if (!d_values || !d_send) return fail(HPXFFT_ERR_INVALID_ARG, "null device buffer");
+    if (((uintptr_t)d_values | (uintptr_t)d_send) & 15) return fail(HPXFFT_ERR_INVALID_ARG, "buffers must be 16-byte aligned");
+    cudaStream_t st = s->rows->stream;
+    cudaError_t e = cudaEventRecord(s->ev[0], st);
+    if (e == cudaSuccess) e = dispatch_rows_only(*s->rows, d_values, d_values);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev[1], st);
+    if (e == cudaSuccess) e = slab_pack(*s, d_values, d_send, st);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev[2], st);
+    if (e != cudaSuccess) return cuda_fail(e, "slab rows");
+    s->ran_rows = true;
+    return HPXFFT_OK;
+}
+
+int hpxfft_slab_columns(hpxfft_slab s, void *d_recv)
+{
+    if (!s) return fail(HPXFFT_ERR_STATE, "null slab");
+    if (!d_recv) return fail(HPXFFT_ERR_INVALID_ARG, "null device buffer");
+    if ((uintptr_t)d_recv & 15) return fail(HPXFFT_ERR_INVALID_ARG, "buffers must be 16-byte aligned");
+    cudaStream_t st = s->cols->stream;
+    cudaError_t e = cudaEventRecord(s->ev[3], st);
+    if (e == cudaSuccess) e = dispatch_columns_only(*s->cols, d_recv);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev[4], st);
+    if (e != cudaSuccess) return cuda_fail(e, "slab columns");
+    s->ran_cols = true;
+    return HPXFFT_OK;
+}
+
+int hpxfft_slab_finish(hpxfft_slab s, const void *d_recv, void *d_values)
+{
+    if (!s) return fail(HPXFFT_ERR_STATE, "null slab");
+    if (!d_recv || !d_values) return fail(HPXFFT_ERR_INVALID_ARG, "null device buffer");
+    if (((uintptr_t)d_recv | (uintptr_t)d_values) & 15) return fail(HPXFFT_ERR_INVALID_ARG, "buffers must be 16-byte aligned");
+    cudaStream_t st = s->rows->stream;
+    cudaError_t e = cudaEventRecord(s->ev[5], st);
+    if (e == cudaSuccess) e = slab_unpack(*s, d_recv, d_values, st);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev[6], st);
+    if (e != cudaSuccess) return cuda_fail(e, "slab finish");
+    s->ran_finish = true;
+    return HPXFFT_OK;
+}
+
+int hpxfft_slab_synchronize(hpxfft_slab s)
+{
+    if (!s) return fail(HPXFFT_ERR_STATE, "null slab");
+    cudaError_t e = cudaStreamSynchronize(s->rows->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "slab");
+    int rc = check_device_error(s->rows);
+    return rc == HPXFFT_OK ? check_device_error(s->cols) : rc;
+}
+
+// Device seconds of the local phases of the last run, with the reference's
+// keys (core/src/distributed/loop.cpp:260-268); the exchanges are the
+// caller's, so first_comm and second_comm are not measured here.
+int hpxfft_slab_get_measurement(hpxfft_slab s, const char *name, double *value)
+{
+    if (!s || !name || !value) return fail(HPXFFT_ERR_INVALID_ARG, "null argument");
+    int rc = hpxfft_slab_synchronize(s);
+    if (rc != HPXFFT_OK) return rc;
+    collect(*s->rows);
+    collect(*s->cols);
+    if (s->ran_rows) {
+        s->meas["first_fftw"] = event_s(s->ev[0], s->ev[1]);
+        s->meas["first_split"] = event_s(s->ev[1], s->ev[2]);
+    }
+    s->meas["first_trans"] = 0.0;  // the received tiles are the column slab
+    if (s->ran_cols) s->meas["second_fftw"] = event_s(s->ev[3], s->ev[4]);
+    s->meas["second_split"] = 0.0;  // the column slab is the send layout
+    if (s->ran_finish) s->meas["second_trans"] = event_s(s->ev[5], s->ev[6]);
+    s->meas["n_ranks"] = (double)s->P;
+    s->meas["rank"] = (double)s->rank;
+    s->meas["tile_columns"] = (double)s->w;
+    auto it = s->meas.find(name);
+    *value = it == s->meas.end() ? 0.0 : it->second;
+    return HPXFFT_OK;
+}
+
+}  // extern "C"

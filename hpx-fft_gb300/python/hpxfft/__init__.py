@@ -12,11 +12,11 @@ Every transform runs in libhpxfft_gb300.so on the GPU; there is no CPU path.
 """
 from . import _capi
 from ._capi import HpxFftError, HpxFftInvalidArgument
-from .plan import Plan, Plan3D
+from .plan import Plan, Plan3D, Slab
 from .batch import Batch
 from . import util, shared, distributed
 
-__all__ = ["Plan", "Plan3D", "Batch", "HpxFftError", "HpxFftInvalidArgument", "util", "shared", "distributed", "_capi",
+__all__ = ["Plan", "Plan3D", "Slab", "Batch", "HpxFftError", "HpxFftInvalidArgument", "util", "shared", "distributed", "_capi",
            "pipe_peaks"]
 
 

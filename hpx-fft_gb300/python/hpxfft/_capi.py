@@ -69,6 +69,15 @@ SIGNATURES = {
     "hpxfft_wisdom_export": (_ci, [_cs]),
     "hpxfft_wisdom_import": (_ci, [_cs]),
     "hpxfft_wisdom_forget": (_ci, []),
+    "hpxfft_slab_create": (_ci, [ctypes.POINTER(_vp), _sz, _sz, _sz, _sz, _ci, _cs]),
+    "hpxfft_slab_destroy": (_ci, [_vp]),
+    "hpxfft_slab_set_stream": (_ci, [_vp, _vp]),
+    "hpxfft_slab_tile_bytes": (_ci, [_vp, ctypes.POINTER(_sz)]),
+    "hpxfft_slab_rows": (_ci, [_vp, _vp, _vp]),
+    "hpxfft_slab_columns": (_ci, [_vp, _vp]),
+    "hpxfft_slab_finish": (_ci, [_vp, _vp, _vp]),
+    "hpxfft_slab_synchronize": (_ci, [_vp]),
+    "hpxfft_slab_get_measurement": (_ci, [_vp, _cs, ctypes.POINTER(ctypes.c_double)]),
     "hpxfft_measure_pipe_peaks": (_ci, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "hpxfft_host_alloc": (_ci, [ctypes.POINTER(_vp), _sz]),
     "hpxfft_host_free": (_ci, [_vp]),

@@ -201,3 +201,62 @@ class Plan3D:
             self.close()
         except Exception:
             pass
+
+
+class Slab:
+    """Local phases of the slab-decomposed 2D r2c on one rank of P
+    (hpxfft_slab_* in the C ABI): rank `rank` holds global rows
+    rank*n_row_local .. of the padded input; send and receive buffers are
+    n_ranks tiles of tile_bytes, tile d for rank d; the caller exchanges
+    them (see hpxfft.distributed.loop)."""
+
+    def __init__(self, n_row_local: int, n_col: int, n_ranks: int, rank: int, precision="f64",
+                 plan_flag: str = "estimate"):
+        lib = _capi.load()
+        self._lib = lib
+        self._h = ctypes.c_void_p()
+        _capi.check(lib.hpxfft_slab_create(ctypes.byref(self._h), n_row_local, n_col, n_ranks, rank,
+                                           precision_code(precision), plan_flag.encode()))
+        n = ctypes.c_size_t()
+        _capi.check(lib.hpxfft_slab_tile_bytes(self._h, ctypes.byref(n)))
+        self.tile_bytes = n.value
+        self.n_row_local, self.n_col, self.n_ranks, self.rank = int(n_row_local), int(n_col), int(n_ranks), int(rank)
+        self.dtype = real_dtype(precision)
+        self.tile_columns = -(-(self.n_col // 2) // self.n_ranks)
+
+    def set_stream(self, handle: int) -> None:
+        _capi.check(self._lib.hpxfft_slab_set_stream(self._h, ctypes.c_void_p(handle)))
+
+    def rows(self, values_ptr: int, send_ptr: int) -> None:
+        _capi.check(self._lib.hpxfft_slab_rows(self._h, ctypes.c_void_p(values_ptr), ctypes.c_void_p(send_ptr)))
+
+    def columns(self, recv_ptr: int) -> None:
+        _capi.check(self._lib.hpxfft_slab_columns(self._h, ctypes.c_void_p(recv_ptr)))
+
+    def finish(self, recv_ptr: int, values_ptr: int) -> None:
+        _capi.check(self._lib.hpxfft_slab_finish(self._h, ctypes.c_void_p(recv_ptr), ctypes.c_void_p(values_ptr)))
+
+    def synchronize(self) -> None:
+        _capi.check(self._lib.hpxfft_slab_synchronize(self._h))
+
+    def measurement(self, name: str) -> float:
+        v = ctypes.c_double()
+        _capi.check(self._lib.hpxfft_slab_get_measurement(self._h, name.encode(), ctypes.byref(v)))
+        return v.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.hpxfft_slab_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -181,6 +181,44 @@ HPXFFT_API int hpxfft_execute3d_r2c(hpxfft_plan3d plan, void *device_values);
  * (axis 0) of the last transform, seconds; other keys as the 2D plan. */
 HPXFFT_API int hpxfft_plan3d_get_measurement(hpxfft_plan3d plan, const char *name, double *value);
 
+/* ---- slab decomposition over P ranks -----------------------------------
+ * The per-locality compute of hpxfft::distributed::loop::fft_2d_r2c
+ * (core/src/distributed/loop.cpp:130-272) for P localities, one GPU each,
+ * with index maps that are right for every P (the reference's transposes,
+ * core/src/distributed/loop.cpp:87-127, interleave the slabs cyclically and
+ * are right only for P = 1).  Rank r holds global rows r*n_row_local .. of
+ * the padded n_row x n_col input (n_row = P * n_row_local).  The dcy =
+ * n_col/2 complex columns split into P tiles of w = ceil(dcy / P) columns
+ * (zero padded), so dcy need not be a multiple of P.  A send or receive
+ * buffer is P tiles of hpxfft_slab_tile_bytes each, tile d for rank d.
+ * The exchanges are the caller's (an all_to_all of equal tiles, or P
+ * scatters); the library runs the local phases, stream-ordered:
+ *   1. hpxfft_slab_rows(values, send): row r2c of the local rows (in place)
+ *      and the pack (core/src/distributed/loop.cpp:19-27 split_vec);
+ *   2. exchange send -> recv (tile d to rank d);
+ *   3. hpxfft_slab_columns(recv): the received tiles are the column slab
+ *      [n_row][w] of this rank's columns; column c2c in place; afterwards
+ *      tile d holds the rows of rank d and is sent back as it is;
+ *   4. exchange recv -> recv2;
+ *   5. hpxfft_slab_finish(recv2, values): the local rows of the spectrum,
+ *      X[r*n_row_local + x][ky], in the padded layout.
+ * Measurements (seconds, last run): "first_fftw", "first_split",
+ * "second_fftw", "second_trans", "plan"; "first_trans" and "second_split"
+ * are 0 (no separate transposes); "first_comm" / "second_comm" belong to
+ * the caller.  Split-BF16 runs FP32 rows and tensor-core columns (n_row a
+ * power of two in [1024, 65536]). */
+typedef struct hpxfft_slab_s *hpxfft_slab;
+HPXFFT_API int hpxfft_slab_create(hpxfft_slab *slab, size_t n_row_local, size_t n_col, size_t n_ranks, size_t rank,
+                                  int precision, const char *plan_flag);
+HPXFFT_API int hpxfft_slab_destroy(hpxfft_slab slab);
+HPXFFT_API int hpxfft_slab_set_stream(hpxfft_slab slab, void *cuda_stream);
+HPXFFT_API int hpxfft_slab_tile_bytes(hpxfft_slab slab, size_t *bytes);
+HPXFFT_API int hpxfft_slab_rows(hpxfft_slab slab, void *device_values, void *device_send);
+HPXFFT_API int hpxfft_slab_columns(hpxfft_slab slab, void *device_recv);
+HPXFFT_API int hpxfft_slab_finish(hpxfft_slab slab, const void *device_recv, void *device_values);
+HPXFFT_API int hpxfft_slab_synchronize(hpxfft_slab slab);
+HPXFFT_API int hpxfft_slab_get_measurement(hpxfft_slab slab, const char *name, double *value);
+
 /* Static description of a status code; message of the calling thread's
  * most recent failure. */
 HPXFFT_API const char *hpxfft_status_string(int status);
