@@ -7,9 +7,9 @@ value = algorithmic HBM bytes per step (4*S, S = nx*(ny/2+1)*16 B: the row
 pass reads and writes S, the column pass reads and writes S) / time.
 
 e2e = the same metric through the C ABI with host buffers
-(hpxfft_execute_r2c_host on a page-locked host array: the row kernel reads
-it and the last column step writes it over the host link, timed from the
-first byte read to the last byte written).
+(hpxfft_execute_r2c_host on a page-locked host array: chunked copies over
+the host link overlapped with the kernels, timed from before the first byte
+leaves the host to after the last byte lands back).
 
 --impl reference times the reference's algorithm on the host cores: the FP64
 C restatement of hpxfft::shared::loop (oracle/), because the reference itself
@@ -358,6 +358,7 @@ def run_ours(args):
     h2d = plan.measurement("h2d")
     d2h = plan.measurement("d2h")
     zero_copy = plan.measurement("host_zero_copy") == 1.0
+    pipelined = plan.measurement("host_pipelined") == 1.0
 
     peak, peak_kind = measured_peak_hbm()
     # per launch: every kernel of the step reads S and writes S (B / 2)
@@ -442,7 +443,10 @@ def run_ours(args):
                 "ms_per_step": 1e3 * e2e_s,
                 "h2d_ms": 1e3 * h2d,
                 "d2h_ms": 1e3 * d2h,
-                "host_path": ("zero-copy: the row pass reads and the last column step writes the page-locked host "
+                "host_path": ("pipelined: 8 strided host-to-device copies (one per group of column-step-A rows) "
+                              "overlapped with the row and step-A kernels, 8 device-to-host copies overlapped with "
+                              "step B" if pipelined else
+                              "zero-copy: the row pass reads and the last column step writes the page-locked host "
                               "buffer over the host link" if zero_copy else "staged through a device buffer"),
             },
             "clocks": clk.summary(),

@@ -200,7 +200,8 @@ __global__ void __launch_bounds__(NV, 2 * 512 / NV) colstep_tc_kernel(TcColStepA
     cpx<float> *s = reinterpret_cast<cpx<float> *>(base);  // FP32 tile once the MMAs are done
 
     const int tid = threadIdx.x;
-    const int g = blockIdx.x / a.strips, col0 = (blockIdx.x % a.strips) * W;
+    const int bx = blockIdx.x + a.block_offset;
+    const int g = bx / a.strips, col0 = (bx % a.strips) * W;
     const float *in = reinterpret_cast<const float *>(a.in) + (long long)blockIdx.y * a.in_bstride;
     float *out = reinterpret_cast<float *>(a.out) + (long long)blockIdx.y * a.out_bstride;
     const cpx<float> *ptab = reinterpret_cast<const cpx<float> *>(a.ptab);
@@ -267,7 +268,7 @@ __global__ void __launch_bounds__(FL * (1 << FW) / 16, 1024 / (FL * (1 << FW) / 
     float2 x[16];
     {
         const bool live = row < a.nrows;
-        const float *src = in + (long long)row * a.in_stride + 2 * (long long)jj;
+        const float *src = in + phys_row(a, row) * a.in_stride + 2 * (long long)jj;
 #pragma unroll
         for (int t = 0; t < 16; ++t) x[t] = live ? ld_stream(src + 2 * (long long)LR * t) : make_float2(0.f, 0.f);
     }
