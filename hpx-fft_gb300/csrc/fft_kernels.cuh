@@ -241,6 +241,24 @@ __device__ void local_fft(cpx<T> *s, int L, int log2W, const PassPlan &pp, const
 // register allocator sees straight-line code.  Twiddles come from per-pass
 // tables laid out [r-1][k] (one coalesced load per r across a warp):
 //   ptab_p[(r-1)*Ls + k] = W_{Ls*R}^{r*k},  r in [1,R), k in [0,Ls).
+__host__ __device__ constexpr int ilog2c(int v)
+{
+    int r = 0;
+    while ((1 << (r + 1)) <= v) ++r;
+    return r;
+}
+
+// Float-float chains (radix 8 first) renormalise their pairs after every
+// second pass only (Ls = 8, 512, ...): the error-free sums and products stay
+// exact on unnormalised pairs, whose low word grows by a few units in the
+// high word's last place in between; every store to global memory
+// renormalises.  Other types: no-op.
+template <class T, int Ls>
+__host__ __device__ constexpr bool renorm_after_pass()
+{
+    return !std::is_same<T, ff>::value || (ilog2c(Ls) / 3) % 2 == 1;
+}
+
 template <class T, int R, int L, int W, int NT, int DIR, int Ls, bool RAW, bool POST>
 __device__ __forceinline__ void fixed_pass(cpx<T> *s, const cpx<T> *__restrict__ tp, const int *sEc,
                                            const cpx<T> *__restrict__ post_tw, int post_mult)
@@ -294,7 +312,12 @@ __device__ __forceinline__ void fixed_pass(cpx<T> *s, const cpx<T> *__restrict__
             const int k = jj % Ls;
             const int base = (jj - k) * R + k;
 #pragma unroll
-            for (int r = 0; r < R; ++r) s[pidx((base + r * Ls) * W + w)] = cnorm(v[t][r]);
+            for (int r = 0; r < R; ++r) {
+                if constexpr (renorm_after_pass<T, Ls>())
+                    s[pidx((base + r * Ls) * W + w)] = cnorm(v[t][r]);
+                else
+                    s[pidx((base + r * Ls) * W + w)] = v[t][r];
+            }
         }
     }
     __syncthreads();
@@ -701,7 +724,7 @@ __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bi
                 }
                 DFT<R1, -1, T>::run(v);
 #pragma unroll
-                for (int r = 0; r < R1; ++r) s[pidx(((jj * R1 + r) << log2W) + w)] = cnorm(v[r]);
+                for (int r = 0; r < R1; ++r) s[pidx(((jj * R1 + r) << log2W) + w)] = v[r];  // pass 0: no renorm
             }
         }
         __syncthreads();
@@ -1454,7 +1477,7 @@ __device__ __forceinline__ void colstep_direct_body(const ColStepArgs &a, int bx
                 }
                 DFT<R1, DIR, T>::run(v);
 #pragma unroll
-                for (int r = 0; r < R1; ++r) s[pidx((jj * R1 + r) * W + w)] = cnorm(v[r]);
+                for (int r = 0; r < R1; ++r) s[pidx((jj * R1 + r) * W + w)] = v[r];  // pass 0: no renorm
             }
         }
     }

@@ -47,7 +47,6 @@ struct TcColStepArgs {
     long long spin_limit;  // polls of the MMA barrier before giving up
 };
 
-__host__ __device__ constexpr int ilog2c(int v) { return v <= 1 ? 0 : 1 + ilog2c(v / 2); }
 
 // Byte offset of (row, 16-byte K chunk) in an operand.
 __device__ __forceinline__ int tc_row_offset(int row, int chunk) { return (row >> 3) * 512 + chunk * 128 + (row & 7) * 16; }

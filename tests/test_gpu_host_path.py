@@ -33,7 +33,7 @@ def test_pinned_and_pageable_match_device(gpu_lib, cuda, prec, nx, ny):
     assert np.array_equal(pinned, ref), prec
 
 
-@pytest.mark.parametrize("prec,nx,ny", [("f64", 16384, 1024), ("f64", 4096, 4096), ("f32", 8192, 2048),
+@pytest.mark.parametrize("prec,nx,ny", [("f64", 16384, 1024), ("f64", 8192, 4096), ("f32", 8192, 2048),
                                         ("bf16x3", 4096, 1024)])
 def test_pipelined_host_path_matches_device_path(gpu_lib, cuda, prec, nx, ny):
     """Chunked copies overlapped with the kernels: same bits as the device
