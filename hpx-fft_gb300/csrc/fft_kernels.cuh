@@ -457,17 +457,9 @@ struct RowArgs {
     int pairs_out;            // float-float r2c: store (hi, lo) pairs and one exponent per row
     int *exp_out;             // [batch][nrows] when pairs_out
     int prefetch;             // persistent r2c: prefetch the next row group into L2 (device input only)
-    // a launch over a subset of the rows (chunked host transfers): with
-    // map_on, logical row i is row map_g0 + (i mod 2^map_lgG) + map_N1 (i div
-    // 2^map_lgG) of the arrays; otherwise row i is row i
-    int map_on, map_lgG, map_g0, map_N1;
+    // exponent slot of row r of batch item b (pairs_out): exp_out[b * exp_bstride + r]
+    long long exp_bstride;
 };
-
-__device__ __forceinline__ long long phys_row(const RowArgs &a, int row)
-{
-    return !a.map_on ? (long long)row
-                     : (long long)a.map_g0 + (row & ((1 << a.map_lgG) - 1)) + (long long)a.map_N1 * (row >> a.map_lgG);
-}
 
 struct ColArgs {
     void *data;               // complex [nx][ncols] rows, in place
@@ -558,12 +550,11 @@ __device__ __forceinline__ void row_r2c_split(const cpx<typename A::T> *s, const
         const cpx<T> zb = cconj(s[pidx((((M - k) % M) << log2W) + w)]);
         const cpx<T> e = chalf(za + zb), o = chalf(za - zb);
         const cpx<T> tk = cmul(tw[k], o);
-        const long long prow = phys_row(a, row);
-        S *orow = out + prow * a.out_stride;
+        S *orow = out + row * a.out_stride;
         if (A::kScaled && a.pairs_out) {
             store_pair<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk));
             if (M - k != k) store_pair<A>(orow + 2 * (long long)(M - k), cconj(e + mul_i<+1>(tk)));
-            if (k == 0) a.exp_out[(long long)bidx * a.nrows + prow] = block_exp(sEc[w]);
+            if (k == 0) a.exp_out[(long long)bidx * a.exp_bstride + row] = block_exp(sEc[w]);
             continue;
         }
         store_c<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk), E);
@@ -611,8 +602,7 @@ __device__ __forceinline__ void row_last_pass_split(const cpx<typename A::T> *s,
         last_task(jj, w, va);
         if (jj2 != jj) last_task(jj2, w, vb);
         const int E = A::kScaled ? scale_exp(sEc[w]) : 0;
-        const long long prow = phys_row(a, row);
-        S *orow = out + prow * a.out_stride;
+        S *orow = out + (long long)row * a.out_stride;
         auto emit = [&](int k, cpx<T> zk, cpx<T> zp) {  // k <= M/2, zp = Z[M - k]
             const cpx<T> zb = cconj(zp);
             const cpx<T> e = chalf(zk + zb), o = chalf(zk - zb);
@@ -620,7 +610,7 @@ __device__ __forceinline__ void row_last_pass_split(const cpx<typename A::T> *s,
             if (A::kScaled && a.pairs_out) {
                 store_pair<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk));
                 if (M - k != k) store_pair<A>(orow + 2 * (long long)(M - k), cconj(e + mul_i<+1>(tk)));
-                if (k == 0) a.exp_out[(long long)bidx * a.nrows + prow] = block_exp(sEc[w]);
+                if (k == 0) a.exp_out[(long long)bidx * a.exp_bstride + row] = block_exp(sEc[w]);
             } else {
                 store_c<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk), E);
                 if (M - k != k) store_c<A>(orow + 2 * (long long)(M - k), cconj(e + mul_i<+1>(tk)), E);
@@ -671,7 +661,7 @@ __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bi
         using V2 = typename std::conditional<sizeof(S) == 8, double2, float2>::type;
         const int w = t & wmask, m = t >> log2W, row = row0 + w;
         V2 v{};
-        if (row < a.nrows) v = ld_stream(in + phys_row(a, row) * a.in_stride + 2 * (crank + (long long)C * m));
+        if (row < a.nrows) v = ld_stream(in + row * a.in_stride + 2 * (crank + (long long)C * m));
         return v;
     };
     if constexpr (kFixed && C == 1) {
@@ -693,7 +683,7 @@ __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bi
             for (int r = 0; r < R1; ++r) {
                 raw[t][r] = V2{};
                 if (active && (NTASK % NT == 0 || task < NTASK) && row < a.nrows)
-                    raw[t][r] = ld_stream(in + phys_row(a, row) * a.in_stride + 2 * (long long)(jj + r * LR1));
+                    raw[t][r] = ld_stream(in + row * a.in_stride + 2 * (long long)(jj + r * LR1));
             }
         }
         if constexpr (A::kScaled) {
@@ -802,14 +792,13 @@ __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bi
             const cpx<T> zb = cconj(*cl.map_shared_rank(&s[pidx(lip)], cp));
             const cpx<T> e = chalf(za + zb), o = chalf(za - zb);
             const cpx<T> tk = cmul(tw[k], o);
-            const long long prow0 = phys_row(a, row0);
-            S *orow = out + prow0 * a.out_stride;
+            S *orow = out + row0 * a.out_stride;
             if (row0 < a.nrows) {
                 if (A::kScaled && a.pairs_out) {
                     store_pair<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk));
                     if (k == 0) {
                         store_pair<A>(orow + 2 * (long long)M, cconj(e + mul_i<+1>(tk)));
-                        a.exp_out[(long long)bidx * a.nrows + prow0] = block_exp(sEc[0]);
+                        a.exp_out[(long long)bidx * a.exp_bstride + row0] = block_exp(sEc[0]);
                     }
                 } else {
                     store_c<A>(orow + 2 * (long long)k, e + mul_i<-1>(tk), E);
@@ -857,12 +846,9 @@ __global__ void HPXFFT_BOUNDS(A, FL) row_r2c_kernel(RowArgs a)
             const int next = group + gridDim.x;
             if (a.prefetch && next < ngroups) {
                 const int r0 = next << log2W, nr = min(1 << log2W, a.nrows - r0);
-                const S *src = reinterpret_cast<const S *>(a.in) + (long long)blockIdx.y * a.in_bstride;
-                if (!a.map_on)
-                    prefetch_l2(src + (long long)r0 * a.in_stride, (long long)nr * a.in_stride * (long long)sizeof(S));
-                else
-                    for (int w = 0; w < nr; ++w)
-                        prefetch_l2(src + phys_row(a, r0 + w) * a.in_stride, a.in_stride * (long long)sizeof(S));
+                const S *src = reinterpret_cast<const S *>(a.in) + (long long)blockIdx.y * a.in_bstride +
+                               (long long)r0 * a.in_stride;
+                prefetch_l2(src, (long long)nr * a.in_stride * (long long)sizeof(S));
             }
             row_r2c_body<A, 1, FL, FW>(a, group, blockIdx.y);
             __syncthreads();  // shared memory is reused by the next group

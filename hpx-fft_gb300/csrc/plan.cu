@@ -422,6 +422,7 @@ static RowArgs row_args(const hpxfft_plan_s &p, const void *in, void *out, int a
     a.ptab = p.row.ptab;
     a.pairs_out = 0;
     a.exp_out = nullptr;
+    a.exp_bstride = (long long)p.nx;
     return a;
 }
 
@@ -581,9 +582,7 @@ static cudaError_t run_inverse(hpxfft_plan_s &p, void *data, int adjoint)
 static bool pipelined_shape(const hpxfft_plan_s &p)
 {
     const int K = hpxfft_plan_s::kChunks;
-    auto pow2 = [](int v) { return v > 0 && !(v & (v - 1)); };
-    return p.col_two_step && p.batch == 1 && !p.columns_only && !p.rows_only && p.N1 % K == 0 && p.N2 % K == 0 &&
-           pow2(p.N1 / K) && pow2(p.N2 / K);
+    return p.col_two_step && p.batch == 1 && !p.columns_only && !p.rows_only && p.N1 % K == 0 && p.N2 % K == 0;
 }
 
 static cudaError_t ensure_pipeline(hpxfft_plan_s &p)
@@ -603,8 +602,6 @@ static cudaError_t run_forward_pipelined(hpxfft_plan_s &p, void *h)
     const int K = hpxfft_plan_s::kChunks;
     const size_t rb = p.ncol * p.real_bytes;  // bytes per row
     const int GA = p.N1 / K, GB = p.N2 / K;
-    int lgGA = 0;
-    while ((1 << lgGA) < GA) ++lgGA;
     char *d = static_cast<char *>(p.dbuf);
     char *hc = static_cast<char *>(h);
     const bool pairs = p.ff_pairs;
@@ -619,24 +616,24 @@ static cudaError_t run_forward_pipelined(hpxfft_plan_s &p, void *h)
         if ((e = cudaEventRecord(p.chunk_in[c], p.copy_in)) != cudaSuccess) return e;
     }
     const int wrows = 1 << p.row.log2W;
-    const int chunk_rows = GA * p.N2;
     const int stripsA = (int)((p.dcy + ((size_t)1 << p.colA.log2W) - 1) >> p.colA.log2W);
     const int stripsB = (int)((p.dcy + ((size_t)1 << p.colB.log2W) - 1) >> p.colB.log2W);
     for (int c = 0; c < K; ++c) {
         if ((e = cudaStreamWaitEvent(p.stream, p.chunk_in[c], 0)) != cudaSuccess) return e;
-        RowArgs ra = row_args(p, d, d, 0);
-        ra.nrows = chunk_rows;
-        ra.map_on = 1;
-        ra.map_lgG = lgGA;
-        ra.map_g0 = c * GA;
-        ra.map_N1 = p.N1;
+        // the chunk's rows as a strided batch: N2 items of GA consecutive
+        // rows, N1 rows apart, starting at row c GA
+        char *d0 = d + c * GA * rb;
+        RowArgs ra = row_args(p, d0, d0, 0);
+        ra.nrows = GA;
+        ra.in_bstride = ra.out_bstride = (long long)p.N1 * (long long)p.ncol;
         ra.prefetch = 1;
         if (pairs) {
             ra.pairs_out = 1;
-            ra.exp_out = p.exp_rows;
+            ra.exp_out = p.exp_rows + c * GA;
+            ra.exp_bstride = p.N1;
         }
         LaunchShape rs = p.row.shape;
-        rs.grid = dim3((unsigned)(((chunk_rows + wrows - 1) / wrows) * p.row.C), 1, 1);
+        rs.grid = dim3((unsigned)(((GA + wrows - 1) / wrows) * p.row.C), (unsigned)p.N2, 1);
         e = p.tc_rows ? TcRowLaunch::run(ra, p.tc_dft, p.dev_error, rs.grid, p.stream)
                       : RowLaunch<A>::r2c(ra, rs, p.row.FL, p.stream);
         if (e != cudaSuccess) return e;

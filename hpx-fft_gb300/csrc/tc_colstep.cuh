@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(FL * (1 << FW) / 16, 1024 / (FL * (1 << FW) / 
     float2 x[16];
     {
         const bool live = row < a.nrows;
-        const float *src = in + phys_row(a, row) * a.in_stride + 2 * (long long)jj;
+        const float *src = in + (long long)row * a.in_stride + 2 * (long long)jj;
 #pragma unroll
         for (int t = 0; t < 16; ++t) x[t] = live ? ld_stream(src + 2 * (long long)LR * t) : make_float2(0.f, 0.f);
     }
