@@ -618,8 +618,9 @@ def extras(torch, hpxfft, args, x64, oracle_ref, peak):
             sec = {"workload": workload_name(nx, ny, prec), "ms": ms, "value": B / (ms * 1e-3) / 1e9, "unit": "GB/s",
                    "frac_of_measured_hbm": B / (ms * 1e-3) / 1e9 / peak}
             if prec == "bf16x3":
-                sec["tensor_core_stage"] = ("first radix-16 pass of the rows and of both column steps, tcgen05 "
-                                            "kind::f16, 3-term BF16 split, FP32 accumulate")
+                sec["tensor_core_stage"] = ("first radix-16 pass of both column steps, tcgen05 kind::f16, 3-term "
+                                            "BF16 split, FP32 accumulate; FP32 rows (the plan's rule: the "
+                                            "tensor-core row measured slower)")
             if oracle_ref is not None:
                 sec["rel_l2_vs_fp64_oracle"], sec["max_abs_err_vs_fp64_oracle"] = _rel_to_oracle(
                     y32.cpu().numpy().view(np.complex64), oracle_ref)

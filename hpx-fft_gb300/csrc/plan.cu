@@ -981,12 +981,14 @@ static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t
                 // rows: the tensor-core r2c where the FP32 plan has a compiled
                 // single-CTA shape of 128..512 vectors; other rows stay FP32
                 // (the launcher sizes its own CTAs; row.shape stays the FP32
-                // one, which the inverse's c2r rows use).  The choice
-                // tc_rows = 0 keeps FP32 rows (16384^2: 0.61 ms against
-                // 0.93 ms for the tensor-core row, whose BF16 split costs
-                // more CUDA-core work than the radix-16 butterfly it replaces)
+                // one, which the inverse's c2r rows use) when the choice
+                // tc_rows = 1 asks for them.  The rule keeps FP32 rows:
+                // 16384^2 rows take 0.54 ms in FP32 against 0.87 ms on the
+                // tensor cores, whose BF16 split costs more CUDA-core work
+                // than the radix-16 butterfly it replaces (the whole
+                // transform: 1.66 against 1.98 ms)
                 if (!columns_only && p->row.FL && TcRowLaunch::supports((int)p->M, p->row.log2W, p->row.C) &&
-                    want.tc_rows != 0)
+                    want.tc_rows == 1)
                     p->tc_rows = true;
             }
         }

@@ -113,7 +113,10 @@ def test_half_occupancy_variant(gpu_lib, cuda, oracle_lib, monkeypatch, nx, ny):
 
 # every compiled tensor-core row shape: M = ny / 2 in 128 .. 8192
 @pytest.mark.parametrize("ny", [256, 512, 1024, 2048, 4096, 8192, 16384])
-def test_tensor_core_rows_vs_oracle(gpu_lib, cuda, oracle_lib, tmp_path, ny):
+def test_tensor_core_rows_vs_oracle(gpu_lib, cuda, oracle_lib, tmp_path, monkeypatch, ny):
+    """Tensor-core rows, which the plan takes when asked (the rule keeps
+    FP32 rows, measured faster)."""
+    monkeypatch.setenv("HPXFFT_TC_ROWS", "1")
     nx = 1024
     with gpu_lib.Plan(nx, 2 * (ny // 2 + 1), 1, "bf16x3", "estimate") as plan:
         plan.write_plan(tmp_path / "plan.txt")
