@@ -76,59 +76,20 @@ __device__ __noinline__ void batch_col(const ColArgs &a, int group)
     col_body<A, 1, -1, FL, FW>(a, group, 0);
 }
 
-// Bring item `it`'s input into L2: the rows of a row group (one contiguous
-// range), or the W-column segment of every row of a column strip (one
-// prefetch per 128-byte line).  A strip prefetched before its instance's
-// rows are done fetches lines those rows rewrite later; L2 keeps them
-// coherent, so the prefetch is only early, never wrong.
-template <class S>
-__device__ __forceinline__ void batch_prefetch(const BatchArgs &b, int it)
-{
-    const BatchItem item = b.items[it];
-    const BatchInst in = b.insts[item.inst];
-    const S *base = reinterpret_cast<const S *>(b.arena) + in.offset;
-    if (item.kind == 0) {
-        const int W = 1 << b.dims[in.row_dim].log2W;
-        const int r0 = item.group * W, nr = min(W, in.nx - r0);
-        prefetch_l2(base + (long long)r0 * in.ncol, (long long)nr * in.ncol * (long long)sizeof(S));
-    } else {
-        const int W = 1 << b.dims[in.col_dim].log2W;
-        const int col0 = item.group * W, ncols = min(W, in.dcy - col0);
-        const int seg = 2 * ncols * (int)sizeof(S);
-        for (int r = threadIdx.x; r < in.nx; r += blockDim.x) {
-            const char *p = reinterpret_cast<const char *>(base + (long long)r * in.ncol + 2 * col0);
-            for (int off = 0; off < seg; off += 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + off));
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(p + seg - 1));
-        }
-    }
-}
-
 // Two CTAs per SM (64 registers, <= 70 KB shared memory each): while one
-// streams an item in or out, the other computes.  Each CTA holds one item
-// of look-ahead: it takes its next item from the queue before transforming
-// the current one and prefetches that item's data into L2.  The waits still
-// end: the earliest unfinished item in queue order is a row item (no wait)
-// or a column item whose rows all precede it; if a CTA holds it as
-// look-ahead, that CTA's current item precedes it and is finished, so the
-// CTA moves on to it.
+// streams an item in or out, the other computes.
 template <class A>
 __global__ void __launch_bounds__(kBatchThreads, 2) batch_kernel(BatchArgs b)
 {
     using T = typename A::T;
     using S = typename A::S;
-    __shared__ int s_item, s_next, s_ok;
+    __shared__ int s_item, s_ok;
     int *next = b.counters, *timeout = b.counters + 1, *rows_done = b.counters + 2;
-    if (threadIdx.x == 0) s_next = atomicAdd(next, 1);
     for (;;) {
-        __syncthreads();  // every thread has read s_next / s_item of the last iteration
-        if (threadIdx.x == 0) {
-            s_item = s_next;
-            s_next = s_item < b.nitems ? atomicAdd(next, 1) : b.nitems;
-        }
+        if (threadIdx.x == 0) s_item = atomicAdd(next, 1);
         __syncthreads();
         const int it = s_item;
         if (it >= b.nitems) return;
-        if (s_next < b.nitems) batch_prefetch<S>(b, s_next);
         const BatchItem item = b.items[it];
         const BatchInst in = b.insts[item.inst];
         S *base = reinterpret_cast<S *>(b.arena) + in.offset;
@@ -207,6 +168,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_kernel(BatchArgs b)
                 if (!done) batch_col<A, 0, 0>(ca, item.group);
             }
         }
+        __syncthreads();  // s_item is rewritten next iteration
     }
 }
 
