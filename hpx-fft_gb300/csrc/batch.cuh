@@ -77,42 +77,85 @@ __device__ __noinline__ void batch_col(const ColArgs &a, int group)
 }
 
 // Two CTAs per SM (64 registers, <= 70 KB shared memory each): while one
-// streams an item in or out, the other computes.
+// streams an item in or out, the other computes.  Thread 0 takes the item,
+// does the bounded wait of a column item and builds the body's arguments in
+// shared memory: one copy per CTA, which the non-inlined bodies read
+// through a reference, instead of one per thread on the thread's stack
+// (local memory, whose traffic to L2 and DRAM outweighed the data's).
 template <class A>
 __global__ void __launch_bounds__(kBatchThreads, 2) batch_kernel(BatchArgs b)
 {
     using T = typename A::T;
     using S = typename A::S;
-    __shared__ int s_item, s_ok;
+    __shared__ int s_item, s_ok, s_kind, s_group, s_fixed;
+    __shared__ RowArgs s_ra;
+    __shared__ ColArgs s_ca;
     int *next = b.counters, *timeout = b.counters + 1, *rows_done = b.counters + 2;
     for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(next, 1);
+        if (threadIdx.x == 0) {
+            const int it = atomicAdd(next, 1);
+            s_item = it;
+            if (it < b.nitems) {
+                const BatchItem item = b.items[it];
+                const BatchInst in = b.insts[item.inst];
+                S *base = reinterpret_cast<S *>(b.arena) + in.offset;
+                const cpx<T> *pool = reinterpret_cast<const cpx<T> *>(b.twpool);
+                s_kind = item.kind;
+                s_group = item.group;
+                s_ok = 1;
+                if (item.kind == 0) {
+                    const BatchDim &d = b.dims[in.row_dim];
+                    RowArgs ra{};
+                    ra.in = base;
+                    ra.out = base;
+                    ra.in_stride = ra.out_stride = in.ncol;
+                    ra.nrows = in.nx;
+                    ra.M = in.M;
+                    ra.log2W = d.log2W;
+                    ra.pp = d.pp;
+                    ra.tw = pool + in.tw_row;
+                    ra.Ltab = 2 * in.M;
+                    ra.ptab = pool + d.ptab;
+                    s_ra = ra;
+                    s_fixed = d.fixed_id;
+                } else {
+                    long long spins = 0;
+                    while (atomicAdd(&rows_done[item.inst], 0) < in.row_items) {
+                        if (++spins > b.spin_limit) {
+                            s_ok = 0;
+                            atomicExch(timeout, 1);
+                            break;
+                        }
+                        __nanosleep(128);
+                    }
+                    __threadfence();
+                    const BatchDim &d = b.dims[in.col_dim];
+                    ColArgs ca{};
+                    ca.data = base;
+                    ca.row_stride = in.ncol;
+                    ca.nx = in.nx;
+                    ca.ncols = in.dcy;
+                    ca.log2W = d.log2W;
+                    ca.pp = d.pp;
+                    ca.tw = pool + in.tw_col;
+                    ca.Ltab = in.nx;
+                    ca.ptab = pool + d.ptab;
+                    s_ca = ca;
+                    s_fixed = d.fixed_id;
+                }
+            }
+        }
         __syncthreads();
         const int it = s_item;
         if (it >= b.nitems) return;
-        const BatchItem item = b.items[it];
-        const BatchInst in = b.insts[item.inst];
-        S *base = reinterpret_cast<S *>(b.arena) + in.offset;
-        const cpx<T> *pool = reinterpret_cast<const cpx<T> *>(b.twpool);
-        if (item.kind == 0) {
-            const BatchDim &d = b.dims[in.row_dim];
-            RowArgs ra{};
-            ra.in = base;
-            ra.out = base;
-            ra.in_stride = ra.out_stride = in.ncol;
-            ra.nrows = in.nx;
-            ra.M = in.M;
-            ra.log2W = d.log2W;
-            ra.pp = d.pp;
-            ra.tw = pool + in.tw_row;
-            ra.Ltab = 2 * in.M;
-            ra.ptab = pool + d.ptab;
+        const int group = s_group, fixed = s_fixed;
+        if (s_kind == 0) {
             bool done = false;
             if constexpr (sizeof(S) == 4) {
-                switch (d.fixed_id) {
+                switch (fixed) {
 #define HPXFFT_X(ID, L_, W_)                                \
     case ID:                                                \
-        batch_row<A, L_, W_>(ra, item.group);               \
+        batch_row<A, L_, W_>(s_ra, group);                  \
         done = true;                                        \
         break;
                     HPXFFT_BATCH_ROWS_F32(HPXFFT_X)
@@ -120,55 +163,27 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_kernel(BatchArgs b)
                 default: break;
                 }
             }
-            if (!done) batch_row<A, 0, 0>(ra, item.group);
+            if (!done) batch_row<A, 0, 0>(s_ra, group);
             __threadfence();
             __syncthreads();
-            if (threadIdx.x == 0) atomicAdd(&rows_done[item.inst], 1);
-        } else {
-            if (threadIdx.x == 0) {
-                int ok = 1;
-                long long spins = 0;
-                while (atomicAdd(&rows_done[item.inst], 0) < in.row_items) {
-                    if (++spins > b.spin_limit) {
-                        ok = 0;
-                        atomicExch(timeout, 1);
-                        break;
-                    }
-                    __nanosleep(128);
-                }
-                __threadfence();
-                s_ok = ok;
-            }
-            __syncthreads();
-            if (s_ok) {
-                const BatchDim &d = b.dims[in.col_dim];
-                ColArgs ca{};
-                ca.data = base;
-                ca.row_stride = in.ncol;
-                ca.nx = in.nx;
-                ca.ncols = in.dcy;
-                ca.log2W = d.log2W;
-                ca.pp = d.pp;
-                ca.tw = pool + in.tw_col;
-                ca.Ltab = in.nx;
-                ca.ptab = pool + d.ptab;
-                bool done = false;
-                if constexpr (sizeof(S) == 4) {
-                    switch (d.fixed_id) {
+            if (threadIdx.x == 0) atomicAdd(&rows_done[b.items[it].inst], 1);
+        } else if (s_ok) {
+            bool done = false;
+            if constexpr (sizeof(S) == 4) {
+                switch (fixed) {
 #define HPXFFT_X(ID, L_, W_)                                  \
     case ID:                                                  \
-        batch_col<A, L_, W_>(ca, item.group);                 \
+        batch_col<A, L_, W_>(s_ca, group);                    \
         done = true;                                          \
         break;
-                        HPXFFT_BATCH_COLS_F32(HPXFFT_X)
+                    HPXFFT_BATCH_COLS_F32(HPXFFT_X)
 #undef HPXFFT_X
-                    default: break;
-                    }
+                default: break;
                 }
-                if (!done) batch_col<A, 0, 0>(ca, item.group);
             }
+            if (!done) batch_col<A, 0, 0>(s_ca, group);
         }
-        __syncthreads();  // s_item is rewritten next iteration
+        __syncthreads();  // the shared arguments are rewritten next iteration
     }
 }
 
