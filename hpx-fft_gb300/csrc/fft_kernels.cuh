@@ -1227,6 +1227,7 @@ struct ColStepArgs {
     // of the launch is block block_offset + b of the full grid of
     // grid_blocks blocks (exponent slots are indexed by the full grid)
     int block_offset, grid_blocks;
+    int warp_local;  // float-float with pair input: the warp-local kernel (colstep_warp_kernel)
 };
 
 template <class A, int DIR, int FL, int FW>
@@ -1321,6 +1322,142 @@ __global__ void HPXFFT_BOUNDS(A, FL) colstep_kernel(ColStepArgs a)
         if (col >= a.ncols) continue;
         const int E = A::kScaled ? (pairs_in ? (Eblk == kExpNone ? 0 : Eblk) : scale_exp(sEc[w])) : 0;
         cpx<T> v = s[pidx(t)];
+        if (a.post && g) v = cmul(v, twid<DIR>(tw, g * k));
+        S *o = out + (out_row0 + (long long)a.out_step * k) * a.row_stride + 2 * (long long)col;
+        if (pairs_out)
+            store_pair<A>(o, v);
+        else
+            store_c<A>(o, v, E);
+    }
+}
+
+// ---------------------------------------------- warp-local column steps
+// The float-float column step with pair input, its passes warp-local: each
+// column of the CTA's strip is owned by TPC = FL / 8 threads of one warp
+// (32 / TPC columns per warp) and kept column-major in shared memory, so
+// the Stockham passes exchange data with __syncwarp only.  The only
+// CTA-wide barriers are after the coalesced load (row segments of the
+// strip into the column-major tile) and before the coalesced store.  Same
+// contract as colstep_kernel for pairs_in = 1 (both forward steps of the
+// float-float pair exchange).
+__host__ __device__ constexpr int wl_col_stride(int L) { return L + L / 16 + 1; }  // odd: load and store conflict-free
+
+template <class T, int R, int L, int DIR, int Ls, int TPC>
+__device__ __forceinline__ void warp_local_pass(cpx<T> *col, int t, const cpx<T> *__restrict__ tp)
+{
+    constexpr int LR = L / R, TPT = LR / TPC;
+    static_assert(LR % TPC == 0, "tasks split evenly over the column's threads");
+    cpx<T> v[TPT][R];
+#pragma unroll
+    for (int u = 0; u < TPT; ++u) {
+        const int jj = t + u * TPC;
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[u][r] = col[pidx(jj + r * LR)];
+        if constexpr (Ls > 1) {
+            const int k = jj % Ls;
+#pragma unroll
+            for (int r = 1; r < R; ++r) v[u][r] = cmul(v[u][r], twid<DIR>(tp, (r - 1) * Ls + k));
+        }
+        DFT<R, DIR, T>::run(v[u]);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int u = 0; u < TPT; ++u) {
+        const int jj = t + u * TPC;
+        const int k = jj % Ls;
+        const int base = (jj - k) * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if constexpr (renorm_after_pass<T, Ls>())
+                col[pidx(base + r * Ls)] = cnorm(v[u][r]);
+            else
+                col[pidx(base + r * Ls)] = v[u][r];
+        }
+    }
+    __syncwarp();
+}
+
+template <class T, int L, int DIR, int MAXR, int Ls, int Off, int TPC>
+struct WarpLocalPasses {
+    static __device__ __forceinline__ void run(cpx<T> *col, int t, const cpx<T> *__restrict__ ptab)
+    {
+        if constexpr (Ls < L) {
+            constexpr int R = fixed_radix(L, Ls, MAXR);
+            warp_local_pass<T, R, L, DIR, Ls, TPC>(col, t, ptab + Off);
+            WarpLocalPasses<T, L, DIR, MAXR, Ls * R, Off + (Ls > 1 ? Ls * (R - 1) : 0), TPC>::run(col, t, ptab);
+        }
+    }
+};
+
+template <class A, int DIR, int FL, int FW>
+__global__ void __launch_bounds__((FL << FW) / A::kEPTFixed, kFixedMinBlocks) colstep_warp_kernel(ColStepArgs a)
+{
+    using T = typename A::T;
+    using S = typename A::S;
+    constexpr int EPT = A::kEPTFixed, W = 1 << FW, NT = (FL << FW) / EPT, TPC = FL / EPT, CS = wl_col_stride(FL);
+    static_assert(32 % TPC == 0 && NT % 32 == 0, "whole columns per warp");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cpx<T> *s = reinterpret_cast<cpx<T> *>(smem_raw);
+    __shared__ int sEm, sExp[kColStepMaxPairL];
+    __shared__ float sFac[kColStepMaxPairL];
+    const int tid = threadIdx.x;
+    const int bx = blockIdx.x + a.block_offset;
+    const int g = bx / a.strips, col0 = (bx % a.strips) * W;
+    const S *in = reinterpret_cast<const S *>(a.in) + (long long)blockIdx.y * a.in_bstride;
+    S *out = reinterpret_cast<S *>(a.out) + (long long)blockIdx.y * a.out_bstride;
+    const cpx<T> *tw = reinterpret_cast<const cpx<T> *>(a.tw);
+    const cpx<T> *ptab = reinterpret_cast<const cpx<T> *>(a.ptab);
+    const long long in_row0 = (long long)g * a.in_gmul, out_row0 = (long long)g * a.out_gmul;
+
+    // exponents of the FL input rows, their maximum, exact power-of-two
+    // factors that bring every row to it (as colstep_kernel)
+    if (tid == 0) sEm = kExpNone;
+    __syncthreads();
+    const int *ein = a.exp_in + (long long)blockIdx.y * a.exp_in_bstride;
+    for (int m = tid; m < FL; m += NT) {
+        const int r = (int)(in_row0 + (long long)a.in_step * m);
+        const int e = ein[(r % a.exp_rmod) * a.exp_rmul + (col0 >> a.exp_cshift)];
+        sExp[m] = e;
+        atomicMax(&sEm, e);
+    }
+    __syncthreads();
+    const int Eblk = sEm;
+    for (int m = tid; m < FL; m += NT) sFac[m] = Eblk == kExpNone ? 1.0f : pow2_le0(sExp[m] - Eblk);
+    __syncthreads();
+
+    // coalesced load: element (m, w) of the strip to column w, position m
+    batched_loop<EPT, double2>(FL << FW, NT,
+                               [&](int t) {
+                                   const int w = t & (W - 1), m = t >> FW, col = col0 + w;
+                                   double2 v{};
+                                   if (col < a.ncols)
+                                       v = ld_stream(in + (in_row0 + (long long)a.in_step * m) * a.row_stride +
+                                                     2 * (long long)col);
+                                   return v;
+                               },
+                               [&](int t, double2 v) {
+                                   const int w = t & (W - 1), m = t >> FW;
+                                   const float4 q = *reinterpret_cast<const float4 *>(&v);
+                                   const float f = sFac[m];
+                                   s[w * CS + pidx(m)] = cpx<T>{ff{q.x * f, q.y * f}, ff{q.z * f, q.w * f}};
+                               });
+    __syncthreads();
+
+    // the column's passes, warp-local
+    {
+        const int c = tid / TPC, t = tid % TPC;
+        WarpLocalPasses<T, FL, DIR, EPT, 1, 0, TPC>::run(s + c * CS, t, ptab);
+    }
+    __syncthreads();
+
+    // coalesced store, times W_nx^(g k) when the step has a post twiddle
+    const bool pairs_out = a.pairs_out != 0;
+    if (pairs_out && tid == 0) a.exp_out[bx + (long long)a.grid_blocks * blockIdx.y] = Eblk;
+    const int E = Eblk == kExpNone ? 0 : Eblk;
+    for (int t = tid; t < (FL << FW); t += NT) {
+        const int w = t & (W - 1), k = t >> FW, col = col0 + w;
+        if (col >= a.ncols) continue;
+        cpx<T> v = s[w * CS + pidx(k)];
         if (a.post && g) v = cmul(v, twid<DIR>(tw, g * k));
         S *o = out + (out_row0 + (long long)a.out_step * k) * a.row_stride + 2 * (long long)col;
         if (pairs_out)

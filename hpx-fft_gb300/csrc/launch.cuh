@@ -335,6 +335,8 @@ cudaError_t ColStepLaunch<A>::prepare()
     if constexpr (sizeof(typename A::S) == 4) {                        \
         HPXFFT_TRY(set_attrs(colstep_direct_kernel<A, -1, L, W>, false));  \
         HPXFFT_TRY(set_attrs(colstep_direct_kernel<A, +1, L, W>, false));  \
+    } else {                                                           \
+        HPXFFT_TRY(set_attrs(colstep_warp_kernel<A, -1, L, W>, false));    \
     }
         if constexpr (sizeof(typename A::S) == 4) {
             HPXFFT_COLSTEP_FIXED_F32(HPXFFT_X)
@@ -377,6 +379,19 @@ cudaError_t ColStepLaunch<A>::run(const ColStepArgs &a, int dir, const LaunchSha
                 HPXFFT_COLSTEP_FIXED_F32(HPXFFT_X)
 #undef HPXFFT_X
                 return cudaErrorInvalidValue;
+            }
+        }
+        if constexpr (sizeof(typename A::S) == 8) {
+            // float-float forward steps with pair input: warp-local passes
+            if (FL && a.pairs_in && a.warp_local && dir < 0) {
+#define HPXFFT_X(L_, W_)                                                                              \
+    if (FL == L_ && a.log2W == W_) {                                                                  \
+        LaunchShape ws = s;                                                                           \
+        ws.smem = (size_t)(1 << W_) * wl_col_stride(L_) * sizeof(cpx<typename A::T>);                 \
+        return launch_cluster(colstep_warp_kernel<A, -1, L_, W_>, a, ws, st);                         \
+    }
+                HPXFFT_COLSTEP_FIXED_FF(HPXFFT_X)
+#undef HPXFFT_X
             }
         }
         if (FL) {

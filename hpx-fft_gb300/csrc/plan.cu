@@ -82,6 +82,9 @@ struct hpxfft_plan_s {
     // float-float forward two-step pass: rows -> step A -> step B exchange
     // raw (hi, lo) pairs with per-row / per-block exponents instead of doubles
     bool ff_pairs = false;
+    // float-float forward column steps with warp-local passes
+    // (HPXFFT_FF_WARP_COLS=0 keeps the CTA-wide passes: tests, tuning)
+    bool ff_warp_cols = true;
     int *exp_rows = nullptr;   // [batch][nx]
     int *exp_step_a = nullptr; // [batch][step A blocks]
     // split-BF16 precision: both column steps (and the rows, for compiled
@@ -485,6 +488,7 @@ static ColStepArgs colstep_args(const hpxfft_plan_s &p, int step, const void *in
     a.ptab = d.ptab;
     a.block_offset = 0;
     a.grid_blocks = (int)d.shape.grid.x;
+    a.warp_local = p.ff_warp_cols ? 1 : 0;
     if (pairs && step == 0) {  // per-row exponents of the row kernel
         a.pairs_in = a.pairs_out = 1;
         a.exp_in = p.exp_rows;
@@ -918,6 +922,7 @@ static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t
     p->tw_elem = f32_storage(precision) ? 8 : 16;
     p->columns_only = columns_only;
     p->rows_only = rows_only;
+    if (const char *v = std::getenv("HPXFFT_FF_WARP_COLS")) p->ff_warp_cols = strcmp(v, "0") != 0;
     const PlanChoice want = merged_choice(forced);
     p->choice.tc_vectors = want.tc_vectors == 512 ? 512 : 256;
     if ((!columns_only && !plan_rows(*p)) || (!rows_only && !plan_cols(*p))) {
