@@ -403,7 +403,8 @@ def run_ours(args):
     steps = int(plan.measurement("column_steps"))
     kernels = {"row_r2c_kernel": stats["first"]}
     if steps == 2:
-        step_kernel = "colstep_tc_kernel" if prec == "bf16x3" else "colstep_kernel"
+        step_kernel = {"bf16x3": "colstep_tc_kernel", "f64": "colstep_warp_kernel",
+                       "f32": "colstep_direct_kernel"}.get(prec, "colstep_kernel")
         kernels[f"{step_kernel} (A)"] = plan.measurement("mean_col_step_a")
         kernels[f"{step_kernel} (B)"] = plan.measurement("mean_col_step_b")
     else:

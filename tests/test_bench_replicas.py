@@ -71,7 +71,7 @@ def test_headline_kernels_have_profiled_traffic():
     at a plausible fraction of the algorithmic bytes per launch (2 S)."""
     bench = _bench()
     alg = 2 * 16384 * 8193 * 16  # read + write of S = nx (ny/2+1) complex doubles
-    for label in ("row_r2c_kernel", "colstep_kernel (A)", "colstep_kernel (B)"):
+    for label in ("row_r2c_kernel", "colstep_warp_kernel (A)", "colstep_warp_kernel (B)"):
         t = bench.profiled_traffic("f64", 16384, 16384, label)
         assert t is not None and 0.8 * alg <= t <= 1.5 * alg, (label, t)
     assert bench.profiled_traffic("f32", 16384, 16384, "row_r2c_kernel") is None
