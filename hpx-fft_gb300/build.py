@@ -32,6 +32,7 @@ SOURCES = [
     "kernels_f64.cu",
     "kernels_tc_cols.cu",
     "twiddles.cu",
+    "bluestein.cu",
     "plan.cu",
     "batch.cu",
     "pipe_peaks.cu",

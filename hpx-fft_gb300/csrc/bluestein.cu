@@ -1,0 +1,409 @@
+// Bluestein's convolution and the transposed row pass: the host-built
+// tables and the elementwise / transposing kernels around the column
+// transforms (the plan logic that strings them together is in plan.cu).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <map>
+#include <mutex>
+#include <utility>
+#include <vector>
+
+#include "bluestein.cuh"
+
+namespace hpxfft_gpu {
+
+// ------------------------------------------------------------ host tables
+
+size_t bluestein_length(size_t L)
+{
+    size_t M = 1;
+    while (M < 2 * L - 1) M <<= 1;
+    return M;
+}
+
+// exp(-2 pi i num / den), 0 <= num < den, in FP64 (angle error below 1e-15)
+static void cis(uint64_t num, uint64_t den, double &re, double &im)
+{
+    const double a = 6.283185307179586476925286766559 * (double)num / (double)den;
+    re = std::cos(a);
+    im = -std::sin(a);
+}
+
+// In-place forward DFT of a power-of-two length: iterative radix-2
+// decimation in time in FP64, twiddles from cos/sin of each angle.
+static void host_fft_pow2(std::vector<double> &re, std::vector<double> &im)
+{
+    const size_t n = re.size();
+    for (size_t i = 1, j = 0; i < n; ++i) {  // bit-reversed order
+        size_t bit = n >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) {
+            std::swap(re[i], re[j]);
+            std::swap(im[i], im[j]);
+        }
+    }
+    std::vector<double> wr(n / 2 + 1), wi(n / 2 + 1);
+    for (size_t k = 0; k < n / 2; ++k) cis(k, n, wr[k], wi[k]);
+    for (size_t len = 2; len <= n; len <<= 1) {
+        const size_t half = len / 2, step = n / len;
+        for (size_t s = 0; s < n; s += len)
+            for (size_t j = 0; j < half; ++j) {
+                const double xr = wr[j * step], xi = wi[j * step];
+                const size_t a = s + j, b = a + half;
+                const double tr = re[b] * xr - im[b] * xi, ti = re[b] * xi + im[b] * xr;
+                re[b] = re[a] - tr;
+                im[b] = im[a] - ti;
+                re[a] += tr;
+                im[a] += ti;
+            }
+    }
+}
+
+// chirp (2 L doubles, interleaved) and kernel (2 M doubles) for (L, M);
+// kernels up to 2^20 entries are kept for the next plan of the same length
+static void host_tables(size_t L, size_t M, std::vector<double> &chirp, std::vector<double> &kernel)
+{
+    static std::mutex mu;
+    static std::map<std::pair<size_t, size_t>, std::vector<double>> cache;
+    chirp.assign(2 * L, 0.0);
+    for (size_t n = 0; n < L; ++n) {
+        const uint64_t r = (uint64_t)((unsigned __int128)n * n % (2 * L));  // n^2 mod 2L
+        cis(r, 2 * L, chirp[2 * n], chirp[2 * n + 1]);
+    }
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = cache.find({L, M});
+        if (it != cache.end()) {
+            kernel = it->second;
+            return;
+        }
+    }
+    std::vector<double> re(M, 0.0), im(M, 0.0);
+    for (size_t m = 0; m < L; ++m) {  // b[m] = b[M - m] = conj c[m]
+        re[m] = chirp[2 * m];
+        im[m] = -chirp[2 * m + 1];
+        if (m) {
+            re[M - m] = re[m];
+            im[M - m] = im[m];
+        }
+    }
+    host_fft_pow2(re, im);
+    kernel.resize(2 * M);
+    const double s = 1.0 / (double)M;
+    for (size_t k = 0; k < M; ++k) {
+        kernel[2 * k] = re[k] * s;
+        kernel[2 * k + 1] = im[k] * s;
+    }
+    if (M <= ((size_t)1 << 20)) {
+        std::lock_guard<std::mutex> lock(mu);
+        cache[{L, M}] = kernel;
+    }
+}
+
+// allocate and fill a device table from interleaved doubles
+static cudaError_t upload(const std::vector<double> &v, bool f32, void **dst)
+{
+    *dst = nullptr;
+    cudaError_t e;
+    if (f32) {
+        std::vector<float> f(v.begin(), v.end());
+        if ((e = cudaMalloc(dst, f.size() * sizeof(float))) != cudaSuccess) return e;
+        e = cudaMemcpy(*dst, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice);
+    } else {
+        if ((e = cudaMalloc(dst, v.size() * sizeof(double))) != cudaSuccess) return e;
+        e = cudaMemcpy(*dst, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) {
+        cudaFree(*dst);
+        *dst = nullptr;
+    }
+    return e;
+}
+
+cudaError_t bluestein_tables(size_t L, size_t M, bool f32, void **chirp, void **kernel)
+{
+    *chirp = *kernel = nullptr;
+    std::vector<double> c, k;
+    host_tables(L, M, c, k);
+    cudaError_t e = upload(c, f32, chirp);
+    if (e == cudaSuccess) e = upload(k, f32, kernel);
+    return e;
+}
+
+cudaError_t split_table(size_t h, bool f32, void **w)
+{
+    std::vector<double> v(2 * (h + 1));
+    for (size_t k = 0; k <= h; ++k) cis(k, 2 * h, v[2 * k], v[2 * k + 1]);
+    return upload(v, f32, w);
+}
+
+// ---------------------------------------------------------------- kernels
+
+template <class V>
+__device__ __forceinline__ V vmul(V a, V b)
+{
+    V r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+
+template <class V>
+__device__ __forceinline__ V vzero()
+{
+    V r;
+    r.x = 0;
+    r.y = 0;
+    return r;
+}
+
+template <class V>
+__device__ __forceinline__ V tab_at(const V *tab, long long i, int conj)
+{
+    V f = tab[i];
+    if (conj) f.y = -f.y;
+    return f;
+}
+
+template <class V>
+__global__ void __launch_bounds__(256) scale_rows_kernel(const V *in, long long in_rs, long long in_bs, V *out,
+                                                         long long out_rs, long long out_bs, const V *tab, int conj,
+                                                         long long rows_in, long long rows_out, long long ncols)
+{
+    const long long b = blockIdx.z;
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= ncols) return;
+    for (long long r = (long long)blockIdx.y * blockDim.y + threadIdx.y; r < rows_out;
+         r += (long long)gridDim.y * blockDim.y) {
+        V v = vzero<V>();
+        if (r < rows_in) v = vmul(in[b * in_bs + r * in_rs + j], tab_at(tab, r, conj));
+        out[b * out_bs + r * out_rs + j] = v;
+    }
+}
+
+// 32 x 32 tiles through shared memory (odd row pitch: no bank conflicts for
+// 8- or 16-byte elements), 256 threads, 4 elements per thread each way;
+// blockIdx.x = row tile * col_tiles + col tile of the destination
+template <class V>
+__global__ void __launch_bounds__(256)
+    transpose_scaled_kernel(const V *src, long long s_rs, long long s_bs, long long src_rows, long long src_cols, V *dst,
+                            long long d_rs, long long d_bs, long long dst_rows, long long dst_cols, unsigned col_tiles,
+                            const V *tab, int tab_on_col, int conj)
+{
+    __shared__ V tile[32][33];
+    const long long r0 = (long long)(blockIdx.x / col_tiles) * 32, c0 = (long long)(blockIdx.x % col_tiles) * 32;
+    const long long b = blockIdx.z;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const long long c = c0 + ty + 8 * q, r = r0 + tx;  // source row c, source column r
+        V v = vzero<V>();
+        if (c < src_rows && r < src_cols) {
+            v = src[b * s_bs + c * s_rs + r];
+            if (tab) v = vmul(v, tab_at(tab, tab_on_col ? c : r, conj));
+        }
+        tile[ty + 8 * q][tx] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const long long r = r0 + ty + 8 * q, c = c0 + tx;
+        if (r < dst_rows && c < dst_cols) dst[b * d_bs + r * d_rs + c] = tile[tx][ty + 8 * q];
+    }
+}
+
+// blockIdx.x = k tile * i_tiles + i tile
+template <class V>
+__global__ void __launch_bounds__(256) r2c_split_kernel(const V *t, long long t_rs, long long t_bs, long long h,
+                                                        const V *chirp, const V *w, V *out, long long o_rs,
+                                                        long long o_bs, long long nrows, unsigned i_tiles)
+{
+    using R = decltype(V{}.x);
+    __shared__ V za[32][33], zb[32][33];
+    const long long k0 = (long long)(blockIdx.x / i_tiles) * 32, i0 = (long long)(blockIdx.x % i_tiles) * 32;
+    const long long b = blockIdx.z;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const long long k = k0 + ty + 8 * q, i = i0 + tx;
+        V a = vzero<V>(), c = vzero<V>();
+        if (k <= h && i < nrows) {
+            const long long ka = k == h ? 0 : k, kb = k == 0 ? 0 : h - k;
+            a = t[b * t_bs + ka * t_rs + i];
+            c = t[b * t_bs + kb * t_rs + i];
+            if (chirp) {
+                a = vmul(a, chirp[ka]);
+                c = vmul(c, chirp[kb]);
+            }
+        }
+        za[ty + 8 * q][tx] = a;
+        zb[ty + 8 * q][tx] = c;
+    }
+    __syncthreads();
+    const R half = (R)0.5;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const long long i = i0 + ty + 8 * q, k = k0 + tx;
+        if (k <= h && i < nrows) {
+            const V a = za[tx][ty + 8 * q], c = zb[tx][ty + 8 * q];  // Z[k], Z[h-k]
+            V e, o;
+            e.x = (a.x + c.x) * half;  // (Z[k] + conj Z[h-k]) / 2
+            e.y = (a.y - c.y) * half;
+            o.x = (a.x - c.x) * half;  // (Z[k] - conj Z[h-k]) / 2
+            o.y = (a.y + c.y) * half;
+            const V wo = vmul(w[k], o);
+            V x;
+            x.x = e.x + wo.y;  // e - i wo
+            x.y = e.y - wo.x;
+            out[b * o_bs + i * o_rs + k] = x;
+        }
+    }
+}
+
+// blockIdx.x = k tile * i_tiles + i tile
+template <class V>
+__global__ void __launch_bounds__(256)
+    c2r_merge_kernel(const V *in, long long i_rs, long long i_bs, long long nrows, long long h, const V *chirp,
+                     const V *w, int adjoint, V *t, long long t_rs, long long t_bs, long long t_rows, long long t_cols,
+                     unsigned i_tiles)
+{
+    using R = decltype(V{}.x);
+    __shared__ V tile[32][33];
+    const long long k0 = (long long)(blockIdx.x / i_tiles) * 32, i0 = (long long)(blockIdx.x % i_tiles) * 32;
+    const long long b = blockIdx.z;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const long long k = k0 + tx, i = i0 + ty + 8 * q;
+        V z = vzero<V>();
+        if (k < h && i < nrows) {
+            V a = in[b * i_bs + i * i_rs + k], c = in[b * i_bs + i * i_rs + (h - k)];
+            if (k == 0) {  // X[0] and X[h]: imaginary parts ignored
+                a.y = 0;
+                c.y = 0;
+            } else if (adjoint) {  // interior bins halved
+                a.x *= (R)0.5;
+                a.y *= (R)0.5;
+                c.x *= (R)0.5;
+                c.y *= (R)0.5;
+            }
+            V s, d;
+            s.x = a.x + c.x;  // X[k] + conj X[h-k]
+            s.y = a.y - c.y;
+            d.x = a.x - c.x;  // X[k] - conj X[h-k]
+            d.y = a.y + c.y;
+            const V wd = vmul(tab_at(w, k, 1), d);
+            z.x = s.x - wd.y;  // s + i wd
+            z.y = s.y + wd.x;
+            if (chirp) z = vmul(z, tab_at(chirp, k, 1));
+        }
+        tile[ty + 8 * q][tx] = z;  // [i][k]
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const long long k = k0 + ty + 8 * q, i = i0 + tx;
+        if (k < t_rows && i < t_cols) t[b * t_bs + k * t_rs + i] = tile[tx][ty + 8 * q];
+    }
+}
+
+// ---------------------------------------------------------------- launchers
+
+static long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
+
+cudaError_t scale_rows(bool f32, const void *in, long long in_rs, long long in_bs, void *out, long long out_rs,
+                       long long out_bs, const void *tab, int conj, long long rows_in, long long rows_out,
+                       long long ncols, int batch, cudaStream_t st)
+{
+    if (rows_out <= 0 || ncols <= 0 || batch <= 0) return cudaSuccess;
+    int bx = 32;
+    while (bx > 1 && bx / 2 >= ncols) bx /= 2;
+    const int by = 256 / bx;
+    const long long gx = ceil_div(ncols, bx);
+    long long gy = ceil_div(rows_out, 4LL * by);
+    if (gy > 65535) gy = 65535;
+    if (gx > 0x7fffffffLL || batch > 65535) return cudaErrorInvalidValue;
+    const dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)batch), block(bx, by);
+    if (f32)
+        scale_rows_kernel<float2><<<grid, block, 0, st>>>((const float2 *)in, in_rs, in_bs, (float2 *)out, out_rs,
+                                                          out_bs, (const float2 *)tab, conj, rows_in, rows_out, ncols);
+    else
+        scale_rows_kernel<double2><<<grid, block, 0, st>>>((const double2 *)in, in_rs, in_bs, (double2 *)out, out_rs,
+                                                           out_bs, (const double2 *)tab, conj, rows_in, rows_out,
+                                                           ncols);
+    return cudaGetLastError();
+}
+
+// tiles of the destination (rows x cols) as one grid dimension
+static bool tile_grid(long long rows, long long cols, int batch, dim3 &grid, unsigned &col_tiles)
+{
+    const long long rt = ceil_div(rows, 32), ct = ceil_div(cols, 32);
+    if (rt * ct > 0x7fffffffLL || ct > 0xffffffffLL || batch > 65535) return false;
+    grid = dim3((unsigned)(rt * ct), 1, (unsigned)batch);
+    col_tiles = (unsigned)ct;
+    return true;
+}
+
+cudaError_t transpose_scaled(bool f32, const void *src, long long s_rs, long long s_bs, long long src_rows,
+                             long long src_cols, void *dst, long long d_rs, long long d_bs, long long dst_rows,
+                             long long dst_cols, const void *tab, int tab_on_col, int conj, int batch,
+                             cudaStream_t st)
+{
+    if (dst_rows <= 0 || dst_cols <= 0 || batch <= 0) return cudaSuccess;
+    dim3 grid;
+    unsigned ct = 0;
+    if (!tile_grid(dst_rows, dst_cols, batch, grid, ct)) return cudaErrorInvalidValue;
+    const dim3 block(32, 8);
+    if (f32)
+        transpose_scaled_kernel<float2><<<grid, block, 0, st>>>((const float2 *)src, s_rs, s_bs, src_rows, src_cols,
+                                                                (float2 *)dst, d_rs, d_bs, dst_rows, dst_cols, ct,
+                                                                (const float2 *)tab, tab_on_col, conj);
+    else
+        transpose_scaled_kernel<double2><<<grid, block, 0, st>>>((const double2 *)src, s_rs, s_bs, src_rows,
+                                                                 src_cols, (double2 *)dst, d_rs, d_bs, dst_rows,
+                                                                 dst_cols, ct, (const double2 *)tab, tab_on_col, conj);
+    return cudaGetLastError();
+}
+
+cudaError_t r2c_split(bool f32, const void *t, long long t_rs, long long t_bs, long long h, const void *chirp,
+                      const void *w, void *out, long long o_rs, long long o_bs, long long nrows, int batch,
+                      cudaStream_t st)
+{
+    if (h <= 0 || nrows <= 0 || batch <= 0) return cudaSuccess;
+    dim3 grid;
+    unsigned it = 0;
+    if (!tile_grid(h + 1, nrows, batch, grid, it)) return cudaErrorInvalidValue;
+    const dim3 block(32, 8);
+    if (f32)
+        r2c_split_kernel<float2><<<grid, block, 0, st>>>((const float2 *)t, t_rs, t_bs, h, (const float2 *)chirp,
+                                                         (const float2 *)w, (float2 *)out, o_rs, o_bs, nrows, it);
+    else
+        r2c_split_kernel<double2><<<grid, block, 0, st>>>((const double2 *)t, t_rs, t_bs, h, (const double2 *)chirp,
+                                                          (const double2 *)w, (double2 *)out, o_rs, o_bs, nrows, it);
+    return cudaGetLastError();
+}
+
+cudaError_t c2r_merge(bool f32, const void *in, long long i_rs, long long i_bs, long long nrows, long long h,
+                      const void *chirp, const void *w, int adjoint, void *t, long long t_rs, long long t_bs,
+                      long long t_rows, long long t_cols, int batch, cudaStream_t st)
+{
+    if (t_rows <= 0 || t_cols <= 0 || batch <= 0) return cudaSuccess;
+    dim3 grid;
+    unsigned it = 0;
+    if (!tile_grid(t_rows, t_cols, batch, grid, it)) return cudaErrorInvalidValue;
+    const dim3 block(32, 8);
+    if (f32)
+        c2r_merge_kernel<float2><<<grid, block, 0, st>>>((const float2 *)in, i_rs, i_bs, nrows, h,
+                                                         (const float2 *)chirp, (const float2 *)w, adjoint,
+                                                         (float2 *)t, t_rs, t_bs, t_rows, t_cols, it);
+    else
+        c2r_merge_kernel<double2><<<grid, block, 0, st>>>((const double2 *)in, i_rs, i_bs, nrows, h,
+                                                          (const double2 *)chirp, (const double2 *)w, adjoint,
+                                                          (double2 *)t, t_rs, t_bs, t_rows, t_cols, it);
+    return cudaGetLastError();
+}
+
+}  // namespace hpxfft_gpu

@@ -22,6 +22,7 @@
 #include <string>
 
 #include "../../include/hpxfft_gb300.h"
+#include "bluestein.cuh"
 #include "launch.cuh"
 
 namespace hpxfft_gpu {
@@ -63,6 +64,22 @@ struct DimPlan {
     int L = 0;
     int FL = 0;              // L when a compile-time pass chain is used, else 0
     void *ptab = nullptr;    // per-pass twiddles of that chain
+};
+
+// A dimension the direct kernels do not cover, run through a columns-only
+// plan `sub` of length M on a scratch array of `width` complex columns:
+// Bluestein's convolution (M the power of two >= 2L - 1) or, for rows
+// longer than a cluster holds, the length-L transform itself (M = L) on a
+// transposed copy.
+struct AltAxis {
+    bool on = false;
+    bool bluestein = false;
+    size_t L = 0, M = 0;
+    size_t width = 0;
+    hpxfft_plan sub = nullptr;
+    void *chirp = nullptr;   // L entries exp(-i pi n^2 / L)
+    void *kernel = nullptr;  // M entries: DFT_M of the conjugate chirp, over M
+    void *wtab = nullptr;    // rows: W_2L^k, k = 0..L
 };
 
 }  // namespace hpxfft_gpu
@@ -122,6 +139,10 @@ struct hpxfft_plan_s {
     // and its best time (ms); empty for "estimate" and for a cached choice
     std::vector<std::pair<std::string, double>> tuning;
     std::string tuned_from;  // "rules", "search" or "wisdom"
+    // rows / columns outside the direct kernels' sizes, and their scratch
+    // array (the two run one after the other on the plan's stream)
+    hpxfft_gpu::AltAxis alt_row, alt_col;
+    void *alt_buf = nullptr;
 };
 
 namespace hpxfft_gpu {
@@ -531,6 +552,89 @@ static cudaError_t run_columns(hpxfft_plan_s &p, void *data, int dir, void *dst)
     return ColStepLaunch<A>::run(colstep_args(p, 1, p.scratch, dst, pairs), dir, p.colB.shape, p.colB.FL, p.stream);
 }
 
+// Bluestein's convolution along the columns of `scr` (M rows of `width`
+// complex values, the chirped input zero-padded): DFT_M, times the kernel's
+// spectrum (conjugated for the inverse), inverse DFT_M.
+template <class A>
+static cudaError_t alt_convolve(hpxfft_plan_s &p, AltAxis &a, void *scr, int dir)
+{
+    const bool f32 = f32_storage(p.prec);
+    const long long w = (long long)a.width, bs = (long long)(a.M * a.width);
+    cudaError_t e = run_columns<A>(*a.sub, scr, -1, scr);
+    if (e == cudaSuccess)
+        e = scale_rows(f32, scr, w, bs, scr, w, bs, a.kernel, dir > 0, (long long)a.M, (long long)a.M, w,
+                       (int)p.batch, p.stream);
+    if (e == cudaSuccess) e = run_columns<A>(*a.sub, scr, +1, scr);
+    return e;
+}
+
+// Columns outside the direct kernels' sizes, in place on `data`: chirp and
+// zero-pad into the scratch array, convolve, chirp back (dir -1 forward,
+// +1 the unnormalised inverse).
+template <class A>
+static cudaError_t run_alt_columns(hpxfft_plan_s &p, void *data, int dir)
+{
+    AltAxis &a = p.alt_col;
+    a.sub->stream = p.stream;
+    const bool f32 = f32_storage(p.prec);
+    const long long dcy = (long long)p.dcy, dbs = (long long)(p.nx * p.dcy), sbs = (long long)(a.M * a.width);
+    const int conj = dir > 0, nb = (int)p.batch;
+    cudaError_t e = scale_rows(f32, data, dcy, dbs, p.alt_buf, dcy, sbs, a.chirp, conj, (long long)p.nx,
+                               (long long)a.M, dcy, nb, p.stream);
+    if (e == cudaSuccess) e = alt_convolve<A>(p, a, p.alt_buf, dir);
+    if (e == cudaSuccess)
+        e = scale_rows(f32, p.alt_buf, dcy, sbs, data, dcy, dbs, a.chirp, conj, (long long)p.nx, (long long)p.nx,
+                       dcy, nb, p.stream);
+    return e;
+}
+
+// Rows outside the direct kernels' sizes, forward, `in` to `out`: the packed
+// rows transposed into the scratch array's columns (chirped and zero-padded
+// for Bluestein), the length-h transforms along them, then the r2c split
+// while transposing back.
+template <class A>
+static cudaError_t run_alt_rows(hpxfft_plan_s &p, const void *in, void *out)
+{
+    AltAxis &a = p.alt_row;
+    a.sub->stream = p.stream;
+    const bool f32 = f32_storage(p.prec);
+    const long long dcy = (long long)p.dcy, dbs = (long long)(p.nx * p.dcy);
+    const long long w = (long long)a.width, tbs = (long long)(a.M * a.width), h = (long long)p.M;
+    const int nb = (int)p.batch;
+    const void *chirp = a.bluestein ? a.chirp : nullptr;
+    cudaError_t e = transpose_scaled(f32, in, dcy, dbs, (long long)p.nx, h, p.alt_buf, w, tbs, (long long)a.M, w,
+                                     chirp, 0, 0, nb, p.stream);
+    if (e == cudaSuccess)
+        e = a.bluestein ? alt_convolve<A>(p, a, p.alt_buf, -1) : run_columns<A>(*a.sub, p.alt_buf, -1, p.alt_buf);
+    if (e == cudaSuccess)
+        e = r2c_split(f32, p.alt_buf, w, tbs, h, chirp, a.wtab, out, dcy, dbs, (long long)p.nx, nb, p.stream);
+    return e;
+}
+
+// The c2r (or its adjoint) of rows outside the direct kernels' sizes, in
+// place: the Hermitian merge while transposing into the scratch array, the
+// inverse length-h transforms along its columns, the packed rows
+// transposed back (pad reals zero).
+template <class A>
+static cudaError_t run_alt_rows_c2r(hpxfft_plan_s &p, void *data, int adjoint)
+{
+    AltAxis &a = p.alt_row;
+    a.sub->stream = p.stream;
+    const bool f32 = f32_storage(p.prec);
+    const long long dcy = (long long)p.dcy, dbs = (long long)(p.nx * p.dcy);
+    const long long w = (long long)a.width, tbs = (long long)(a.M * a.width), h = (long long)p.M;
+    const int nb = (int)p.batch;
+    const void *chirp = a.bluestein ? a.chirp : nullptr;
+    cudaError_t e = c2r_merge(f32, data, dcy, dbs, (long long)p.nx, h, chirp, a.wtab, adjoint, p.alt_buf, w, tbs,
+                              (long long)a.M, w, nb, p.stream);
+    if (e == cudaSuccess)
+        e = a.bluestein ? alt_convolve<A>(p, a, p.alt_buf, +1) : run_columns<A>(*a.sub, p.alt_buf, +1, p.alt_buf);
+    if (e == cudaSuccess)
+        e = transpose_scaled(f32, p.alt_buf, w, tbs, h, (long long)p.nx, data, dcy, dbs, (long long)p.nx, dcy, chirp,
+                             1, 1, nb, p.stream);
+    return e;
+}
+
 // Rows from `in` to `out`, columns on `out`; with the two-step column pass
 // the last step writes `final_out` when it is given (the host buffer of the
 // zero-copy path).
@@ -547,14 +651,17 @@ static cudaError_t run_forward(hpxfft_plan_s &p, const void *in, void *out, void
         ra.pairs_out = 1;
         ra.exp_out = p.exp_rows;
     }
-    if (p.tc_rows)
+    if (p.alt_row.on)
+        e = run_alt_rows<A>(p, in, out);
+    else if (p.tc_rows)
         e = TcRowLaunch::run(ra, p.tc_dft, p.dev_error, p.row.shape.grid, p.stream);
     else
         e = RowLaunch<A>::r2c(ra, p.row.shape, p.row.FL, p.stream);
     if (e != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
     void *dst = final_out && p.col_two_step ? final_out : out;
-    if ((e = run_columns<A>(p, out, -1, dst)) != cudaSuccess) return e;
+    if ((e = p.alt_col.on ? run_alt_columns<A>(p, out, -1) : run_columns<A>(p, out, -1, dst)) != cudaSuccess)
+        return e;
     if ((e = cudaEventRecord(ev[2], p.stream)) != cudaSuccess) return e;
     ++p.next;
     return cudaSuccess;
@@ -566,10 +673,12 @@ static cudaError_t run_inverse(hpxfft_plan_s &p, void *data, int adjoint)
     cudaError_t e;
     cudaEvent_t *ev = next_slot(p);
     if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
-    if ((e = run_columns<A>(p, data, +1, data)) != cudaSuccess) return e;
-    if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
-    if ((e = RowLaunch<A>::c2r(row_args(p, data, data, adjoint), p.row.shape, p.row.FL, p.stream)) != cudaSuccess)
+    if ((e = p.alt_col.on ? run_alt_columns<A>(p, data, +1) : run_columns<A>(p, data, +1, data)) != cudaSuccess)
         return e;
+    if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
+    e = p.alt_row.on ? run_alt_rows_c2r<A>(p, data, adjoint)
+                     : RowLaunch<A>::c2r(row_args(p, data, data, adjoint), p.row.shape, p.row.FL, p.stream);
+    if (e != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[2], p.stream)) != cudaSuccess) return e;
     ++p.next;
     return cudaSuccess;
@@ -586,7 +695,8 @@ static cudaError_t run_inverse(hpxfft_plan_s &p, void *data, int adjoint)
 static bool pipelined_shape(const hpxfft_plan_s &p)
 {
     const int K = hpxfft_plan_s::kChunks;
-    return p.col_two_step && p.batch == 1 && !p.columns_only && !p.rows_only && p.N1 % K == 0 && p.N2 % K == 0;
+    return p.col_two_step && p.batch == 1 && !p.columns_only && !p.rows_only && !p.alt_row.on && p.N1 % K == 0 &&
+           p.N2 % K == 0;
 }
 
 static cudaError_t ensure_pipeline(hpxfft_plan_s &p)
@@ -701,7 +811,8 @@ static cudaError_t run_columns_only(hpxfft_plan_s &p, void *data)
     cudaEvent_t *ev = next_slot(p);
     if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
-    if ((e = run_columns<A>(p, data, -1, data)) != cudaSuccess) return e;
+    if ((e = p.alt_col.on ? run_alt_columns<A>(p, data, -1) : run_columns<A>(p, data, -1, data)) != cudaSuccess)
+        return e;
     if ((e = cudaEventRecord(ev[2], p.stream)) != cudaSuccess) return e;
     ++p.next;
     return cudaSuccess;
@@ -717,7 +828,8 @@ static cudaError_t run_rows_only(hpxfft_plan_s &p, const void *in, void *out)
     if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
     RowArgs ra = row_args(p, in, out, 0);
     ra.prefetch = 1;
-    if ((e = RowLaunch<A>::r2c(ra, p.row.shape, p.row.FL, p.stream)) != cudaSuccess) return e;
+    e = p.alt_row.on ? run_alt_rows<A>(p, in, out) : RowLaunch<A>::r2c(ra, p.row.shape, p.row.FL, p.stream);
+    if (e != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[2], p.stream)) != cudaSuccess) return e;
     ++p.next;
@@ -883,14 +995,79 @@ static PlanChoice merged_choice(const PlanChoice &forced)
 
 }  // namespace hpxfft_gpu
 
+static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batch, int precision,
+                            const char *plan_flag, int mode, const PlanChoice &forced, bool allow_alt = true);
+
+// Longest n_row for rows outside the direct kernels' sizes (the transposing
+// kernels tile n_row in 32-row tiles on one grid dimension with the others).
+constexpr size_t kAltMaxRows = (size_t)1 << 21;
+
+static int alt_sub_plan(hpxfft_plan_s &p, size_t len, size_t width, hpxfft_plan *sub)
+{
+    return create_plan_with(sub, len, 2 * width, p.batch, p.prec, "estimate", kPlanColumns, PlanChoice{}, false);
+}
+
+// Rows outside the direct kernels' sizes: the column kernels of length
+// h = ny/2 on a transposed copy when such a plan exists, else Bluestein.
+static int setup_alt_rows(hpxfft_plan_s &p)
+{
+    AltAxis &a = p.alt_row;
+    const bool f32 = f32_storage(p.prec);
+    a.L = p.M;
+    a.width = (std::max<size_t>(p.nx, 2) + 3) / 4 * 4;  // 64-byte rows of the scratch array start aligned
+    int rc = alt_sub_plan(p, a.L, a.width, &a.sub);
+    if (rc == HPXFFT_OK) {
+        a.M = a.L;
+    } else if (rc == HPXFFT_ERR_UNSUPPORTED_SIZE) {
+        a.bluestein = true;
+        a.M = bluestein_length(a.L);
+        if ((rc = alt_sub_plan(p, a.M, a.width, &a.sub)) != HPXFFT_OK) return rc;
+        cudaError_t e = bluestein_tables(a.L, a.M, f32, &a.chirp, &a.kernel);
+        if (e != cudaSuccess) return cuda_fail(e, "Bluestein tables");
+    } else {
+        return rc;
+    }
+    cudaError_t e = split_table(a.L, f32, &a.wtab);
+    return e == cudaSuccess ? HPXFFT_OK : cuda_fail(e, "split twiddles");
+}
+
+// Columns outside the direct kernels' sizes: Bluestein over the dcy columns.
+static int setup_alt_cols(hpxfft_plan_s &p)
+{
+    AltAxis &a = p.alt_col;
+    a.L = p.nx;
+    a.width = p.dcy;
+    a.bluestein = true;
+    a.M = bluestein_length(a.L);
+    int rc = alt_sub_plan(p, a.M, a.width, &a.sub);
+    if (rc != HPXFFT_OK) return rc;
+    cudaError_t e = bluestein_tables(a.L, a.M, f32_storage(p.prec), &a.chirp, &a.kernel);
+    return e == cudaSuccess ? HPXFFT_OK : cuda_fail(e, "Bluestein tables");
+}
+
+static void free_alt(AltAxis &a)
+{
+    if (a.sub) {
+        a.sub->stream = a.sub->own_stream;
+        hpxfft_plan_destroy(a.sub);
+    }
+    cudaFree(a.chirp);
+    cudaFree(a.kernel);
+    cudaFree(a.wtab);
+    a = AltAxis{};
+}
+
 // mode kPlanColumns: a plan of the column pass alone (c2c along n_row of
 // n_col/2 complex columns), the last axis of a 3D transform or the column
 // slab of a slab decomposition; no row plan, no row twiddles, no
 // float-float pair exchange.  kPlanRows: the row pass alone (FP32 rows for
 // split-BF16), the local rows of a slab decomposition.  `forced` sets the
 // tunable choices (-1: the rules); the environment overrides both.
+// Dimensions outside the direct kernels' sizes take the paths of AltAxis
+// (not for split-BF16, and not when allow_alt is false: the sub-plans of
+// those paths).
 static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t batch, int precision,
-                            const char *plan_flag, int mode, const PlanChoice &forced)
+                            const char *plan_flag, int mode, const PlanChoice &forced, bool allow_alt)
 {
     const bool columns_only = mode == kPlanColumns, rows_only = mode == kPlanRows;
     if (!out) return fail(HPXFFT_ERR_INVALID_ARG, "plan pointer is null");
@@ -925,10 +1102,23 @@ static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t
     if (const char *v = std::getenv("HPXFFT_FF_WARP_COLS")) p->ff_warp_cols = strcmp(v, "0") != 0;
     const PlanChoice want = merged_choice(forced);
     p->choice.tc_vectors = want.tc_vectors == 512 ? 512 : 256;
-    if ((!columns_only && !plan_rows(*p)) || (!rows_only && !plan_cols(*p))) {
-        delete p;
-        return fail(HPXFFT_ERR_UNSUPPORTED_SIZE,
-                    "sizes must have no prime factor above 13 and fit the per-cluster shared memory");
+    const bool rows_ok = columns_only || plan_rows(*p);
+    bool cols_ok = rows_only || plan_cols(*p);
+    // power-of-two columns longer than a cluster holds: the two-kernel pass
+    bool steps_only = false;
+    if (!cols_ok && precision != HPXFFT_PREC_F64_NATIVE && precision != HPXFFT_PREC_BF16X3 && want.columns != 1 &&
+        plan_colsteps(*p))
+        cols_ok = steps_only = true;
+    if (!rows_ok || !cols_ok) {
+        if (!allow_alt || precision == HPXFFT_PREC_BF16X3 || (!rows_ok && n_row > kAltMaxRows)) {
+            delete p;
+            return fail(HPXFFT_ERR_UNSUPPORTED_SIZE,
+                        allow_alt ? "sizes outside the direct kernels need a precision other than split-BF16 and "
+                                    "n_row <= 2^21 for long or prime-factor rows"
+                                  : "sizes must have no prime factor above 13 and fit the per-cluster shared memory");
+        }
+        p->alt_row.on = !rows_ok;
+        p->alt_col.on = !cols_ok;
     }
     cudaError_t e = prepare_prec(precision);
     if (e != cudaSuccess) {
@@ -951,19 +1141,20 @@ static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t
             hpxfft_plan_destroy(p);
             return cuda_fail(e, "event");
         }
-    if ((!columns_only && cudaMalloc(&p->tw_row, p->tw_elem * 2 * p->M) != cudaSuccess) ||
-        (!rows_only && cudaMalloc(&p->tw_col, p->tw_elem * p->nx) != cudaSuccess)) {
+    const bool direct_rows = !columns_only && !p->alt_row.on, direct_cols = !rows_only && !p->alt_col.on;
+    if ((direct_rows && cudaMalloc(&p->tw_row, p->tw_elem * 2 * p->M) != cudaSuccess) ||
+        (direct_cols && cudaMalloc(&p->tw_col, p->tw_elem * p->nx) != cudaSuccess)) {
         hpxfft_plan_destroy(p);
         return fail(HPXFFT_ERR_ALLOC, "twiddle tables");
     }
-    int rc = columns_only ? HPXFFT_OK : setup_fixed(*p, p->row, true, p->stream);
-    if (rc == HPXFFT_OK && !rows_only) rc = setup_fixed(*p, p->col, false, p->stream);
+    int rc = direct_rows ? setup_fixed(*p, p->row, true, p->stream) : HPXFFT_OK;
+    if (rc == HPXFFT_OK && direct_cols && !steps_only) rc = setup_fixed(*p, p->col, false, p->stream);
     // column strategy: the two-kernel pass streams 512-byte row segments and
     // wins once the cluster kernel needs 8 or more CTAs per strip (the rule;
     // the plan's choice may set either)
-    bool want_steps = p->col.C >= 8;
-    if (want.columns == 1) want_steps = false;
-    if (want.columns == 2) want_steps = true;
+    bool want_steps = steps_only || (direct_cols && p->col.C >= 8);
+    if (want.columns == 1 && !steps_only) want_steps = false;
+    if (want.columns == 2 && direct_cols) want_steps = true;
     if (rows_only) want_steps = false;
     if (precision == HPXFFT_PREC_BF16X3 && !rows_only) {
         // the tensor-core stage lives in the column steps: nx = N1 * N2 with
@@ -1010,9 +1201,11 @@ static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t
             }
         }
     }
+    if (rc == HPXFFT_OK && steps_only && !p->col_two_step)
+        rc = fail(HPXFFT_ERR_UNSUPPORTED_SIZE, "no column plan for this n_row");
     // float-float pair exchange between the forward kernels (compiled step
     // shapes only); the choice ff_pairs = 0 keeps doubles in between
-    if (rc == HPXFFT_OK && !columns_only && precision == HPXFFT_PREC_F64 && p->col_two_step && p->colA.FL && p->colB.FL &&
+    if (rc == HPXFFT_OK && direct_rows && precision == HPXFFT_PREC_F64 && p->col_two_step && p->colA.FL && p->colB.FL &&
         p->colA.L <= kColStepMaxPairL && p->colB.L <= kColStepMaxPairL && want.ff_pairs != 0) {
         if (cudaMalloc(&p->exp_rows, sizeof(int) * p->nx * p->batch) != cudaSuccess ||
             cudaMalloc(&p->exp_step_a, sizeof(int) * p->colA.shape.grid.x * p->batch) != cudaSuccess) {
@@ -1027,11 +1220,27 @@ static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t
         hpxfft_plan_destroy(p);
         return fail(rc, msg);
     }
-    if ((!columns_only && (e = gen_twiddles(precision, p->tw_row, (int)(2 * p->M), p->stream)) != cudaSuccess) ||
-        (!rows_only && (e = gen_twiddles(precision, p->tw_col, (int)p->nx, p->stream)) != cudaSuccess) ||
+    if ((direct_rows && (e = gen_twiddles(precision, p->tw_row, (int)(2 * p->M), p->stream)) != cudaSuccess) ||
+        (direct_cols && (e = gen_twiddles(precision, p->tw_col, (int)p->nx, p->stream)) != cudaSuccess) ||
         (e = cudaStreamSynchronize(p->stream)) != cudaSuccess) {
         hpxfft_plan_destroy(p);
         return cuda_fail(e, "twiddle generation");
+    }
+    // the sub-plans, tables and scratch array of the other paths
+    if (p->alt_row.on) rc = setup_alt_rows(*p);
+    if (rc == HPXFFT_OK && p->alt_col.on) rc = setup_alt_cols(*p);
+    if (rc == HPXFFT_OK && (p->alt_row.on || p->alt_col.on)) {
+        const size_t cr = p->alt_row.on ? p->alt_row.M * p->alt_row.width : 0;
+        const size_t cc = p->alt_col.on ? p->alt_col.M * p->alt_col.width : 0;
+        if (cudaMalloc(&p->alt_buf, std::max(cr, cc) * 2 * p->real_bytes * p->batch) != cudaSuccess) {
+            cudaGetLastError();
+            rc = fail(HPXFFT_ERR_ALLOC, "scratch array");
+        }
+    }
+    if (rc != HPXFFT_OK) {
+        std::string msg = g_last_error;
+        hpxfft_plan_destroy(p);
+        return fail(rc, msg);
     }
     {
         int dev = 0, clock_khz = 0, bus_bits = 0;
@@ -1049,6 +1258,11 @@ static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t
     const double f_r2c = 2.5 * ny * std::log2(ny), f_c2c = nx > 1 ? 5.0 * nx * std::log2(nx) : 0.0;
     p->meas["plan_flops"] = ny * f_r2c + nx * f_c2c;
     p->meas["plan_flops_actual"] = (nx * f_r2c + (double)p->dcy * f_c2c) * (double)batch;
+    // which path each pass takes: Bluestein's convolution length (0: none),
+    // rows on a transposed copy (1) or in the row kernel (0)
+    p->meas["bluestein_rows"] = p->alt_row.bluestein ? (double)p->alt_row.M : 0.0;
+    p->meas["bluestein_columns"] = p->alt_col.bluestein ? (double)p->alt_col.M : 0.0;
+    p->meas["transposed_rows"] = p->alt_row.on ? 1.0 : 0.0;
     // the choices in effect
     p->choice.columns = p->col_two_step ? 2 : 1;
     p->choice.ff_pairs = p->ff_pairs ? 1 : 0;
@@ -1162,7 +1376,9 @@ static void clear_trial_state(hpxfft_plan q)
     q->sum_first = q->sum_second = q->sum_total = q->sum_step_a = 0.0;
     q->nsum = 0;
     std::map<std::string, double> keep;
-    for (const char *k : {"plan", "plan_flops", "plan_flops_actual"}) keep[k] = q->meas[k];
+    for (const char *k : {"plan", "plan_flops", "plan_flops_actual", "bluestein_rows", "bluestein_columns",
+                          "transposed_rows"})
+        keep[k] = q->meas[k];
     q->meas.swap(keep);
 }
 
@@ -1436,6 +1652,9 @@ int hpxfft_plan_destroy(hpxfft_plan p)
     cudaFree(p->dev_error);
     cudaFree(p->exp_rows);
     cudaFree(p->exp_step_a);
+    free_alt(p->alt_row);
+    free_alt(p->alt_col);
+    cudaFree(p->alt_buf);
     for (auto &slot : p->kev)
         for (auto &ev : slot)
             if (ev) cudaEventDestroy(ev);
@@ -1520,7 +1739,10 @@ int hpxfft_execute_r2c_host(hpxfft_plan p, void *h)
     cudaError_t e;
     if ((rc = collect(*p)) != HPXFFT_OK) return rc;
     if ((e = cudaEventRecord(p->ev_copy[0], p->stream)) != cudaSuccess) return cuda_fail(e, "event");
-    void *hd = ((uintptr_t)h & 15) ? nullptr : mapped_host(h);
+    // page-locked memory read and written in place by the kernels, except by
+    // the paths of dimensions outside the direct kernels' sizes
+    const bool alt = p->alt_row.on || p->alt_col.on;
+    void *hd = ((uintptr_t)h & 15) || alt ? nullptr : mapped_host(h);
     const bool pipelined = hd && pipelined_shape(*p);
     if (pipelined) {
         // page-locked memory, two-step column plan: chunked copies overlapped
@@ -1650,8 +1872,22 @@ int hpxfft_write_plan(hpxfft_plan p, const char *path)
     if (!p || !path) return fail(HPXFFT_ERR_INVALID_ARG, "null argument");
     FILE *f = fopen(path, "a");
     if (!f) return fail(HPXFFT_ERR_IO, std::string("Failed to open file: ") + path);
-    fprintf(f, "GPU r2c 1D plan:\n%s\n", describe(*p, p->row, "r2c", p->ny).c_str());
-    if (p->col_two_step) {
+    auto columns_of = [](const hpxfft_plan_s &q, const char *what) {
+        if (!q.col_two_step) return describe(q, q.col, what, q.nx);
+        return describe(q, q.colA, "c2c-stepA", (size_t)q.N2) + "\n" + describe(q, q.colB, "c2c-stepB", (size_t)q.N1);
+    };
+    if (p->alt_row.on && p->alt_row.bluestein)
+        fprintf(f, "GPU r2c 1D plan (rows transposed into columns; Bluestein, length %zu through %zu):\n%s\n", p->ny / 2,
+                p->alt_row.M, columns_of(*p->alt_row.sub, "c2c").c_str());
+    else if (p->alt_row.on)
+        fprintf(f, "GPU r2c 1D plan (rows transposed into columns, length %zu):\n%s\n", p->ny / 2,
+                columns_of(*p->alt_row.sub, "c2c").c_str());
+    else
+        fprintf(f, "GPU r2c 1D plan:\n%s\n", describe(*p, p->row, "r2c", p->ny).c_str());
+    if (p->alt_col.on) {
+        fprintf(f, "GPU c2c 1D plan (Bluestein, length %zu through %zu):\n%s\n\n", p->nx, p->alt_col.M,
+                columns_of(*p->alt_col.sub, "c2c").c_str());
+    } else if (p->col_two_step) {
         fprintf(f, "GPU c2c 1D plan (four-step, %d x %d%s):\n%s\n%s\n\n", p->N1, p->N2,
                 p->ff_pairs ? ", float-float pairs between kernels" : "",
                 describe(*p, p->colA, "c2c-stepA", (size_t)p->N2).c_str(),

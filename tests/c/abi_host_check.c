@@ -33,7 +33,7 @@ int main(void)
 
     /* sizes decided before any device call */
     CHECK(hpxfft_plan_create(&plan, 4, 5, 1, HPXFFT_PREC_F64, "estimate") == HPXFFT_ERR_UNSUPPORTED_SIZE);
-    CHECK(hpxfft_plan_create(&plan, 17, 6, 1, HPXFFT_PREC_F32, "estimate") == HPXFFT_ERR_UNSUPPORTED_SIZE);
+    CHECK(hpxfft_plan_create(&plan, 1024, 36, 1, HPXFFT_PREC_BF16X3, "estimate") == HPXFFT_ERR_UNSUPPORTED_SIZE);
     CHECK(hpxfft_plan_create(&plan, 1000, 6, 1, HPXFFT_PREC_BF16X3, "estimate") == HPXFFT_ERR_UNSUPPORTED_SIZE);
     CHECK(hpxfft_plan_create(&plan, 0, 6, 1, HPXFFT_PREC_F64, "estimate") == HPXFFT_ERR_INVALID_ARG);
     CHECK(hpxfft_plan_create(NULL, 4, 6, 1, HPXFFT_PREC_F64, "estimate") == HPXFFT_ERR_INVALID_ARG);

@@ -56,10 +56,17 @@ def test_3d_batch_and_large(gpu_lib, cuda):
     assert rel(run3d(gpu_lib, cuda, x, "f64"), np.fft.rfftn(x)) <= 1e-12
 
 
+def test_3d_prime_lengths(gpu_lib, cuda):
+    """Primes above 13 along each axis: Bluestein's convolution in the slab
+    plan's rows and columns and in the column pass along axis 0."""
+    rng = np.random.default_rng(5)
+    for shape in ((17, 6, 8), (4, 19, 8), (6, 10, 34), (17, 23, 38)):
+        x = rng.uniform(-1, 1, shape)
+        assert rel(run3d(gpu_lib, cuda, x, "f64"), np.fft.rfftn(x)) <= 1e-12, shape
+
+
 def test_3d_argument_errors(gpu_lib, cuda):
     with pytest.raises(gpu_lib.HpxFftError):
         gpu_lib.Plan3D(0, 4, 6)
-    with pytest.raises(gpu_lib.HpxFftError):
-        gpu_lib.Plan3D(17, 4, 6)  # prime factor above 13 along axis 0
     with pytest.raises(gpu_lib.HpxFftError):
         gpu_lib.Plan3D(70000, 4, 6)  # n0 * batch above 65535

@@ -227,10 +227,12 @@ def test_backward_matches_oracle_adjoint(gpu_lib, cuda, oracle_lib, prec):
         assert rel_l2(got[:, :ny], ref[:, :ny]) <= tol, (nx, ny)
 
 
-def test_unsupported_factor_is_rejected(gpu_lib, cuda):
-    for n_row, n_col in ((17, 16), (16, 36), (19 * 2, 8)):  # primes above 13
+def test_split_bf16_rejects_sizes_outside_the_direct_kernels(gpu_lib, cuda):
+    """Primes above 13 take Bluestein's convolution in FP64 and FP32
+    (test_gpu_bluestein.py); split-BF16 keeps the direct kernels' sizes."""
+    for n_row, n_col in ((1024, 36), (17, 16), (1024 * 17, 8)):
         with pytest.raises(gpu_lib.HpxFftError) as e:
-            gpu_lib.Plan(n_row, n_col, 1, "f64", "estimate")
+            gpu_lib.Plan(n_row, n_col, 1, "bf16x3", "estimate")
         assert e.value.status == gpu_lib._capi.HPXFFT_ERR_UNSUPPORTED_SIZE
 
 

@@ -70,7 +70,9 @@ def full_input(nx, ny, seed, f32=False):
 @pytest.mark.parametrize("prec", ["f64", "f32"])
 def test_slab_kernels_match_oracle(gpu_lib, cuda, oracle_lib, prec):
     for nx, ny, P in ((8, 12, 2), (12, 20, 3), (64, 96, 2), (64, 96, 4), (96, 160, 3), (1024, 1024, 4),
-                      (256, 4096, 8), (2048, 64, 2), (16, 30, 1)):
+                      (256, 4096, 8), (2048, 64, 2), (16, 30, 1),
+                      # primes above 13: Bluestein in the local rows and the column slab
+                      (34, 38, 2), (51, 46, 3)):
         x = full_input(nx, ny, nx + ny + P, prec != "f64")
         got, meas = run_emulated(gpu_lib, cuda, x, P, prec)
         ref = oracle_lib.fft_2d_r2c(x.copy(), nthreads=8)

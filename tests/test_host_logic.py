@@ -289,14 +289,19 @@ def test_cpp_dropin_host_side(gpu_lib, build_mod, tmp_path):
 def test_planner_size_limits_before_any_device_call(gpu_lib):
     """The planner's size boundary, decided on the host: shapes it cannot run
     return UNSUPPORTED_SIZE before the first CUDA call; shapes it plans get
-    past planning (OK with a GPU, the CUDA status without one).  Limits:
-    prime factors up to 13; rows of up to 8192 complex values per CTA on a
-    cluster of up to 4, columns of up to 4096 (FP64) or 8192 (FP32) per CTA
-    on a cluster of up to 16, the length divisible by C^2 on a cluster of C;
-    split-BF16 n_row a power of two in [1024, 65536]."""
+    past planning (OK with a GPU, the CUDA status without one).  The direct
+    kernels take prime factors up to 13 with rows of up to 8192 complex
+    values per CTA on a cluster of up to 4 and columns of up to 4096 (FP64)
+    or 8192 (FP32) per CTA on a cluster of up to 16; power-of-two columns
+    beyond that take the two-kernel pass, every other length Bluestein's
+    convolution or (long smooth rows) the column kernels on a transposed
+    copy.  Rejected: odd ny, split-BF16 n_row outside the powers of two in
+    [1024, 65536] or rows outside the direct kernels, and n_row above 2^21
+    with rows outside the direct kernels."""
     capi = gpu_lib._capi
     lib = capi.load()
     F64, F32, BF = capi.PREC_F64, capi.PREC_F32, capi.PREC_BF16X3
+    F64_NATIVE = capi.PREC_F64_NATIVE
 
     def status(n_row, ny, prec):
         h = ctypes.c_void_p()
@@ -309,10 +314,13 @@ def test_planner_size_limits_before_any_device_call(gpu_lib):
                (4, 65536, F32), (65536, 6, F64), (131072, 6, F32), (6, 2 * 3 * 5 * 7 * 11, F32),
                (1024, 6, BF), (65536, 6, BF),
                # longer than one CTA: split over C CTAs, the length divisible by C^2
-               (5005, 6, F32), (3 * 4096, 6, F64), (4, 2 * 5005, F64), (4, 2 * 3 * 8192, F64)]
-    rejected = [(4, 34, F64), (17, 6, F64), (4, 2 * 19, F32), (23, 6, F32), (4, 131072, F32), (4, 131072, F64),
-                (131072, 6, F64), (262144, 6, F32), (512, 6, BF), (1000, 6, BF), (3072, 6, BF), (131072, 6, BF),
-                (5005, 6, F64), (2 * 5005, 6, F64), (2 * 5005, 6, F32), (4, 2 * 9009, F64), (4, 4 * 9009, F32)]
+               (5005, 6, F32), (3 * 4096, 6, F64), (4, 2 * 5005, F64), (4, 2 * 3 * 8192, F64),
+               # Bluestein, the two-kernel pass alone, rows on a transposed copy
+               (4, 34, F64), (17, 6, F64), (4, 2 * 19, F32), (23, 6, F32), (4, 131072, F32), (4, 131072, F64),
+               (131072, 6, F64), (262144, 6, F32), (5005, 6, F64), (2 * 5005, 6, F64), (2 * 5005, 6, F32),
+               (4, 2 * 9009, F64), (4, 4 * 9009, F32), (17, 34, F64_NATIVE), (1 << 21, 34, F32)]
+    rejected = [(512, 6, BF), (1000, 6, BF), (3072, 6, BF), (131072, 6, BF), (1024, 34, BF),
+                ((1 << 21) + 1, 34, F64), (1 << 22, 2 * 3 * 5 * 7 * 11 * 13 * 3, F32)]
     for shape in planned:
         assert status(*shape) != capi.HPXFFT_ERR_UNSUPPORTED_SIZE, shape
     for shape in rejected:
