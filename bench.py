@@ -608,11 +608,55 @@ def cufft_side(torch, stream, x64, nx, ny, steps, warm, oracle_ref, peak):
     return res
 
 
+def prime_sizes(torch, hpxfft, stream, steps, warm, peak):
+    """16381 x 16382 (16381 and ny/2 = 8191 prime): Bluestein's convolution
+    on both passes, FP64 (float-float) and FP32, beside cuFFT on the same
+    input.  The error reference is cuFFT's FP64 output (the oracle's O(p^2)
+    radix-p step is too slow at this size); value uses the same 4 S bytes."""
+    nx, ny = 16381, 16382
+    nc = 2 * (ny // 2 + 1)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(16381)
+    x = torch.rand((nx, ny), generator=g, device="cuda", dtype=torch.float64) * 2 - 1
+    ref = torch.fft.rfft2(x)
+    res = {"workload": f"2d_r2c_{nx}x{ny}", "cufft": {}}
+    for prec, dt, rb in (("f64", torch.float64, 8), ("f32", torch.float32, 4)):
+        B = algorithmic_bytes(nx, ny, rb)
+        xin = torch.zeros((nx, nc), dtype=dt, device="cuda")
+        xin[:, :ny] = x.to(dt)
+        xout = torch.empty_like(xin)
+        with hpxfft.Plan(nx, nc, 1, prec, "estimate") as p:
+            p.set_stream(stream.cuda_stream)
+            ms = _time_steps(torch, stream, lambda: p.execute_oop(xin.data_ptr(), xout.data_ptr()), steps, warm)
+            p.synchronize()
+            got = torch.view_as_complex(xout.view(nx, nc // 2, 2).to(torch.float64))
+            res[prec] = {"ms": ms, "value": B / (ms * 1e-3) / 1e9, "unit": "GB/s",
+                         "frac_of_measured_hbm": B / (ms * 1e-3) / 1e9 / peak,
+                         "bluestein_rows": p.measurement("bluestein_rows"),
+                         "bluestein_columns": p.measurement("bluestein_columns"),
+                         "rel_l2_vs_cufft_f64": float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))}
+        del xin, xout, got
+        xs = x.to(dt)
+        holder = {}
+
+        def step():
+            holder["y"] = torch.fft.rfft2(xs)
+
+        ms = _time_steps(torch, stream, step, steps, warm)
+        res["cufft"][prec] = {"ms": ms, "value": B / (ms * 1e-3) / 1e9, "unit": "GB/s"}
+        del xs, holder
+        torch.cuda.empty_cache()
+    del x, ref
+    torch.cuda.empty_cache()
+    return res
+
+
 def extras(torch, hpxfft, args, x64, oracle_ref, peak):
     """The other workloads of this path, measured in the same run:
     FP32 at the same size (precision), 1024 uneven FP32 transforms in one
-    persistent graph-replayed launch (batching), and the adjoint on 64 FP32
-    2048^2 arrays (differentiation)."""
+    persistent graph-replayed launch (batching), the adjoint on 64 FP32
+    2048^2 arrays (differentiation), and a shape with prime lengths
+    (Bluestein's convolution on both passes)."""
     out = {}
     stream = torch.cuda.current_stream()
     nx, ny = args.nx, args.ny
@@ -666,6 +710,8 @@ def extras(torch, hpxfft, args, x64, oracle_ref, peak):
                     y32.cpu().numpy().view(np.complex64), oracle_ref)
             out[f"precision_{prec}"] = sec
     del x32, y32
+
+    out["prime_sizes"] = prime_sizes(torch, hpxfft, stream, steps, warm, peak)
 
     # batching: 1024 uneven FP32 instances; "measure": the plan step times
     # queue orders once and caches the winner

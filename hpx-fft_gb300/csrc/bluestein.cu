@@ -104,12 +104,21 @@ static void host_tables(size_t L, size_t M, std::vector<double> &chirp, std::vec
 }
 
 // allocate and fill a device table from interleaved doubles
-static cudaError_t upload(const std::vector<double> &v, bool f32, void **dst)
+static cudaError_t upload(const std::vector<double> &v, int fmt, void **dst)
 {
     *dst = nullptr;
     cudaError_t e;
-    if (f32) {
-        std::vector<float> f(v.begin(), v.end());
+    if (fmt == kTabF32 || fmt == kTabFF) {
+        // float-float: each double d as hi = fl(d), lo = fl(d - hi)
+        std::vector<float> f(fmt == kTabFF ? 2 * v.size() : v.size());
+        for (size_t i = 0; i < v.size(); ++i) {
+            if (fmt == kTabF32) {
+                f[i] = (float)v[i];
+            } else {
+                f[2 * i] = (float)v[i];
+                f[2 * i + 1] = (float)(v[i] - (double)f[2 * i]);
+            }
+        }
         if ((e = cudaMalloc(dst, f.size() * sizeof(float))) != cudaSuccess) return e;
         e = cudaMemcpy(*dst, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice);
     } else {
@@ -123,13 +132,13 @@ static cudaError_t upload(const std::vector<double> &v, bool f32, void **dst)
     return e;
 }
 
-cudaError_t bluestein_tables(size_t L, size_t M, bool f32, void **chirp, void **kernel)
+cudaError_t bluestein_tables(size_t L, size_t M, int fmt, void **chirp, void **kernel)
 {
     *chirp = *kernel = nullptr;
     std::vector<double> c, k;
     host_tables(L, M, c, k);
-    cudaError_t e = upload(c, f32, chirp);
-    if (e == cudaSuccess) e = upload(k, f32, kernel);
+    cudaError_t e = upload(c, fmt, chirp);
+    if (e == cudaSuccess) e = upload(k, fmt, kernel);
     return e;
 }
 
@@ -137,7 +146,7 @@ cudaError_t split_table(size_t h, bool f32, void **w)
 {
     std::vector<double> v(2 * (h + 1));
     for (size_t k = 0; k <= h; ++k) cis(k, 2 * h, v[2 * k], v[2 * k + 1]);
-    return upload(v, f32, w);
+    return upload(v, f32 ? kTabF32 : kTabF64, w);
 }
 
 // ---------------------------------------------------------------- kernels

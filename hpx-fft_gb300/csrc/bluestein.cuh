@@ -33,10 +33,15 @@ namespace hpxfft_gpu {
 // Smallest power of two >= 2 L - 1: the convolution length for length L.
 size_t bluestein_length(size_t L);
 
-// Device tables for length L, convolution length M (storage precision):
+// Element formats of the device tables: FP32 or FP64 complex (the storage
+// types, for the kernels below), float-float complex (hi, lo per part: the
+// compute type of the float-float column steps, which apply the factors).
+enum TableFormat { kTabF32 = 0, kTabF64 = 1, kTabFF = 2 };
+
+// Device tables for length L, convolution length M:
 // chirp[n] = exp(-i pi n^2 / L), n < L, and kernel[k] = DFT_M(b)[k] / M, k < M.
 // Allocates both (cudaMalloc); the caller frees them.
-cudaError_t bluestein_tables(size_t L, size_t M, bool f32, void **chirp, void **kernel);
+cudaError_t bluestein_tables(size_t L, size_t M, int fmt, void **chirp, void **kernel);
 
 // Device table w[k] = W_2h^k = exp(-i pi k / h), k = 0..h (the r2c split of
 // rows of 2h reals).  Allocates; the caller frees.

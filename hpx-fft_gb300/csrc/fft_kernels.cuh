@@ -1228,7 +1228,24 @@ struct ColStepArgs {
     // grid_blocks blocks (exponent slots are indexed by the full grid)
     int block_offset, grid_blocks;
     int warp_local;  // float-float with pair input: the warp-local kernel (colstep_warp_kernel)
+    // per-row complex factors in the compute type (Bluestein's convolution):
+    // input row r is multiplied by pre_tab[r] and rows r >= pre_rows read as
+    // zero without a load; output row r is multiplied by post_tab[r] and
+    // rows r >= post_rows are not written; both conjugated when tab_conj.
+    // Null: none.  Only colstep_kernel applies them (the launcher picks it
+    // whenever a table is given).
+    const void *pre_tab, *post_tab;
+    int pre_rows, post_rows;
+    int tab_conj;
 };
+
+// tab[i], conjugated when conj
+template <class T>
+__device__ __forceinline__ cpx<T> row_factor(const cpx<T> *tab, long long i, int conj)
+{
+    const cpx<T> f = tab[i];
+    return conj ? cconj(f) : f;
+}
 
 template <class A, int DIR, int FL, int FW>
 __global__ void HPXFFT_BOUNDS(A, FL) colstep_kernel(ColStepArgs a)
@@ -1251,11 +1268,20 @@ __global__ void HPXFFT_BOUNDS(A, FL) colstep_kernel(ColStepArgs a)
     const long long in_row0 = (long long)g * a.in_gmul, out_row0 = (long long)g * a.out_gmul;
 
     using V2 = typename std::conditional<sizeof(S) == 8, double2, float2>::type;
+    const cpx<T> *pre = reinterpret_cast<const cpx<T> *>(a.pre_tab);
+    const cpx<T> *post = reinterpret_cast<const cpx<T> *>(a.post_tab);
     auto ld = [&](int t) {
         const int w = t & wmask, m = t >> log2W, col = col0 + w;
+        const long long row = in_row0 + (long long)a.in_step * m;
         V2 v{};
-        if (col < a.ncols) v = ld_stream(in + (in_row0 + (long long)a.in_step * m) * a.row_stride + 2 * (long long)col);
+        if (col < a.ncols && (!pre || row < a.pre_rows)) v = ld_stream(in + row * a.row_stride + 2 * (long long)col);
         return v;
+    };
+    // element t of the tile times its input row's factor (rows past
+    // pre_rows were loaded as zero)
+    auto pre_mul = [&](int t, cpx<T> v) {
+        const long long row = in_row0 + (long long)a.in_step * (t >> log2W);
+        return row < a.pre_rows ? cmul(v, row_factor(pre, row, a.tab_conj)) : v;
     };
     int Eblk = kExpNone;  // pair format: the block's common exponent
     bool loaded = false;
@@ -1296,22 +1322,29 @@ __global__ void HPXFFT_BOUNDS(A, FL) colstep_kernel(ColStepArgs a)
             emax = max(emax, max(dbl_biased_exp(v.x), dbl_biased_exp(v.y)));
         });
         reduce_exponents<1>(emax, log2W, sE, sEc);
-        if constexpr (!kFixed) {
+        // the runtime chain converts here; the compiled one in its first
+        // pass, unless input factors need the pairs first
+        if (!kFixed || pre) {
             for (int t = t0; t < nel; t += nth) {
                 const double2 v = reinterpret_cast<double2 *>(s)[pidx(t)];
                 const int E = scale_exp(sEc[t & wmask]);
-                s[pidx(t)] = cpx<ff>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
+                const cpx<ff> c{ff_from_double(v.x, E), ff_from_double(v.y, E)};
+                s[pidx(t)] = pre ? pre_mul(t, c) : c;
             }
         }
     } else {
         batched_loop<EPT, V2>(nel, nth, ld, [&](int t, V2 v) { s[pidx(t)] = cpx<T>{(T)v.x, (T)v.y}; });
+        if (pre) {  // a pass of its own: the batched loads keep their registers
+            __syncthreads();
+            for (int t = t0; t < nel; t += nth) s[pidx(t)] = pre_mul(t, s[pidx(t)]);
+        }
     }
     __syncthreads();
 
     const bool pairs_in = A::kScaled && kFixed && a.pairs_in;
     if constexpr (kFixed)
         FixedPasses<T, FL, (1 << FW), fixed_threads(FL, FW, EPT), DIR, EPT, 1, 0, A::kScaled, false>::run(
-            s, ptab, pairs_in ? nullptr : sEc, tw, 0);
+            s, ptab, pairs_in || pre ? nullptr : sEc, tw, 0);
     else
         local_fft<T, DIR>(s, L, log2W, a.pp, tw, a.Ltab);
 
@@ -1323,7 +1356,12 @@ __global__ void HPXFFT_BOUNDS(A, FL) colstep_kernel(ColStepArgs a)
         const int E = A::kScaled ? (pairs_in ? (Eblk == kExpNone ? 0 : Eblk) : scale_exp(sEc[w])) : 0;
         cpx<T> v = s[pidx(t)];
         if (a.post && g) v = cmul(v, twid<DIR>(tw, g * k));
-        S *o = out + (out_row0 + (long long)a.out_step * k) * a.row_stride + 2 * (long long)col;
+        const long long orow = out_row0 + (long long)a.out_step * k;
+        if (post) {
+            if (orow >= a.post_rows) continue;
+            v = cmul(v, row_factor(post, orow, a.tab_conj));
+        }
+        S *o = out + orow * a.row_stride + 2 * (long long)col;
         if (pairs_out)
             store_pair<A>(o, v);
         else

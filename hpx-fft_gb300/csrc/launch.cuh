@@ -370,8 +370,11 @@ cudaError_t ColStepLaunch<A>::run(const ColStepArgs &a, int dir, const LaunchSha
         // FP32: register-fed first and last passes (16384^2 steps 0.58 / 0.53
         // -> 0.46 / 0.40 ms); float-float is arithmetic-bound and measured no
         // faster that way, so it keeps the staged kernel
+        // per-row factors (Bluestein): the staged kernel, whose registers
+        // hold them without spilling
+        const bool row_factors = a.pre_tab || a.post_tab;
         if constexpr (sizeof(typename A::S) == 4) {
-            if (FL) {
+            if (FL && !row_factors) {
 #define HPXFFT_X(L_, W_)                                                                   \
     if (FL == L_ && a.log2W == W_)                                                         \
         return dir < 0 ? launch_cluster(colstep_direct_kernel<A, -1, L_, W_>, a, s, st)     \
@@ -383,7 +386,7 @@ cudaError_t ColStepLaunch<A>::run(const ColStepArgs &a, int dir, const LaunchSha
         }
         if constexpr (sizeof(typename A::S) == 8) {
             // float-float forward steps with pair input: warp-local passes
-            if (FL && a.pairs_in && a.warp_local && dir < 0) {
+            if (FL && a.pairs_in && a.warp_local && dir < 0 && !row_factors) {
 #define HPXFFT_X(L_, W_)                                                                              \
     if (FL == L_ && a.log2W == W_) {                                                                  \
         LaunchShape ws = s;                                                                           \

@@ -77,9 +77,15 @@ struct AltAxis {
     size_t L = 0, M = 0;
     size_t width = 0;
     hpxfft_plan sub = nullptr;
-    void *chirp = nullptr;   // L entries exp(-i pi n^2 / L)
+    void *chirp = nullptr;   // L entries exp(-i pi n^2 / L) (storage type)
     void *kernel = nullptr;  // M entries: DFT_M of the conjugate chirp, over M
     void *wtab = nullptr;    // rows: W_2L^k, k = 0..L
+    // the same two tables in the column steps' compute type (float-float
+    // pairs for the FP64 plan, the same arrays for FP32): the steps apply
+    // them while loading and storing when the sub-plan takes the two-kernel
+    // pass (fused)
+    void *chirp_c = nullptr, *kernel_c = nullptr;
+    bool fused = false;
 };
 
 }  // namespace hpxfft_gpu
@@ -552,18 +558,47 @@ static cudaError_t run_columns(hpxfft_plan_s &p, void *data, int dir, void *dst)
     return ColStepLaunch<A>::run(colstep_args(p, 1, p.scratch, dst, pairs), dir, p.colB.shape, p.colB.FL, p.stream);
 }
 
+// Both steps of a two-step sub-plan q from `in` to `out` (batch strides of
+// their own, q's row stride), with per-row factors on step A's input
+// (rows past pre_rows read as zero) and on step B's output (rows past
+// post_rows not written).
+template <class A>
+static cudaError_t run_steps_with(hpxfft_plan_s &q, const void *in, long long in_bs, void *out, long long out_bs,
+                                  int dir, const void *pre, int pre_rows, const void *post, int post_rows, int conj)
+{
+    ColStepArgs sa = colstep_args(q, 0, in, q.scratch);
+    sa.in_bstride = in_bs;
+    sa.pre_tab = pre;
+    sa.pre_rows = pre_rows;
+    sa.tab_conj = conj;
+    cudaError_t e = ColStepLaunch<A>::run(sa, dir, q.colA.shape, q.colA.FL, q.stream);
+    if (e != cudaSuccess) return e;
+    ColStepArgs sb = colstep_args(q, 1, q.scratch, out);
+    sb.out_bstride = out_bs;
+    sb.post_tab = post;
+    sb.post_rows = post_rows;
+    sb.tab_conj = conj;
+    return ColStepLaunch<A>::run(sb, dir, q.colB.shape, q.colB.FL, q.stream);
+}
+
 // Bluestein's convolution along the columns of `scr` (M rows of `width`
 // complex values, the chirped input zero-padded): DFT_M, times the kernel's
-// spectrum (conjugated for the inverse), inverse DFT_M.
+// spectrum (conjugated for the inverse; fused into the forward pass's last
+// step when the sub-plan has two), inverse DFT_M.
 template <class A>
 static cudaError_t alt_convolve(hpxfft_plan_s &p, AltAxis &a, void *scr, int dir)
 {
     const bool f32 = f32_storage(p.prec);
     const long long w = (long long)a.width, bs = (long long)(a.M * a.width);
+    const int M = (int)a.M, conj = dir > 0;
+    if (a.fused) {
+        cudaError_t e = run_steps_with<A>(*a.sub, scr, bs, scr, bs, -1, nullptr, 0, a.kernel_c, M, conj);
+        return e == cudaSuccess ? run_steps_with<A>(*a.sub, scr, bs, scr, bs, +1, nullptr, 0, nullptr, 0, 0) : e;
+    }
     cudaError_t e = run_columns<A>(*a.sub, scr, -1, scr);
     if (e == cudaSuccess)
-        e = scale_rows(f32, scr, w, bs, scr, w, bs, a.kernel, dir > 0, (long long)a.M, (long long)a.M, w,
-                       (int)p.batch, p.stream);
+        e = scale_rows(f32, scr, w, bs, scr, w, bs, a.kernel, conj, (long long)a.M, (long long)a.M, w, (int)p.batch,
+                       p.stream);
     if (e == cudaSuccess) e = run_columns<A>(*a.sub, scr, +1, scr);
     return e;
 }
@@ -579,6 +614,16 @@ static cudaError_t run_alt_columns(hpxfft_plan_s &p, void *data, int dir)
     const bool f32 = f32_storage(p.prec);
     const long long dcy = (long long)p.dcy, dbs = (long long)(p.nx * p.dcy), sbs = (long long)(a.M * a.width);
     const int conj = dir > 0, nb = (int)p.batch;
+    if (a.fused) {
+        // chirp and zero-padding in step A's loads, the kernel's spectrum in
+        // step B's stores, the chirp back in the inverse's step B (which
+        // writes only the nx rows of `data`)
+        const int L = (int)p.nx, M = (int)a.M;
+        cudaError_t e = run_steps_with<A>(*a.sub, data, dbs, p.alt_buf, sbs, -1, a.chirp_c, L, a.kernel_c, M, conj);
+        return e == cudaSuccess
+                   ? run_steps_with<A>(*a.sub, p.alt_buf, sbs, data, dbs, +1, nullptr, 0, a.chirp_c, L, conj)
+                   : e;
+    }
     cudaError_t e = scale_rows(f32, data, dcy, dbs, p.alt_buf, dcy, sbs, a.chirp, conj, (long long)p.nx,
                                (long long)a.M, dcy, nb, p.stream);
     if (e == cudaSuccess) e = alt_convolve<A>(p, a, p.alt_buf, dir);
@@ -1007,6 +1052,23 @@ static int alt_sub_plan(hpxfft_plan_s &p, size_t len, size_t width, hpxfft_plan 
     return create_plan_with(sub, len, 2 * width, p.batch, p.prec, "estimate", kPlanColumns, PlanChoice{}, false);
 }
 
+// Bluestein tables for a.L, a.M in the storage type and, for the fused
+// path, in the column steps' compute type.
+static int alt_tables(hpxfft_plan_s &p, AltAxis &a)
+{
+    const bool f32 = f32_storage(p.prec);
+    cudaError_t e = bluestein_tables(a.L, a.M, f32 ? kTabF32 : kTabF64, &a.chirp, &a.kernel);
+    if (e != cudaSuccess) return cuda_fail(e, "Bluestein tables");
+    a.fused = a.sub->col_two_step && !a.sub->tc_cols && p.prec != HPXFFT_PREC_F64_NATIVE;
+    if (f32) {
+        a.chirp_c = a.chirp;
+        a.kernel_c = a.kernel;
+    } else if (a.fused && (e = bluestein_tables(a.L, a.M, kTabFF, &a.chirp_c, &a.kernel_c)) != cudaSuccess) {
+        return cuda_fail(e, "Bluestein tables");
+    }
+    return HPXFFT_OK;
+}
+
 // Rows outside the direct kernels' sizes: the column kernels of length
 // h = ny/2 on a transposed copy when such a plan exists, else Bluestein.
 static int setup_alt_rows(hpxfft_plan_s &p)
@@ -1022,8 +1084,7 @@ static int setup_alt_rows(hpxfft_plan_s &p)
         a.bluestein = true;
         a.M = bluestein_length(a.L);
         if ((rc = alt_sub_plan(p, a.M, a.width, &a.sub)) != HPXFFT_OK) return rc;
-        cudaError_t e = bluestein_tables(a.L, a.M, f32, &a.chirp, &a.kernel);
-        if (e != cudaSuccess) return cuda_fail(e, "Bluestein tables");
+        if ((rc = alt_tables(p, a)) != HPXFFT_OK) return rc;
     } else {
         return rc;
     }
@@ -1040,9 +1101,7 @@ static int setup_alt_cols(hpxfft_plan_s &p)
     a.bluestein = true;
     a.M = bluestein_length(a.L);
     int rc = alt_sub_plan(p, a.M, a.width, &a.sub);
-    if (rc != HPXFFT_OK) return rc;
-    cudaError_t e = bluestein_tables(a.L, a.M, f32_storage(p.prec), &a.chirp, &a.kernel);
-    return e == cudaSuccess ? HPXFFT_OK : cuda_fail(e, "Bluestein tables");
+    return rc == HPXFFT_OK ? alt_tables(p, a) : rc;
 }
 
 static void free_alt(AltAxis &a)
@@ -1051,6 +1110,8 @@ static void free_alt(AltAxis &a)
         a.sub->stream = a.sub->own_stream;
         hpxfft_plan_destroy(a.sub);
     }
+    if (a.chirp_c != a.chirp) cudaFree(a.chirp_c);
+    if (a.kernel_c != a.kernel) cudaFree(a.kernel_c);
     cudaFree(a.chirp);
     cudaFree(a.kernel);
     cudaFree(a.wtab);
