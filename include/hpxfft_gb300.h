@@ -41,7 +41,7 @@ extern "C" {
 typedef enum {
     HPXFFT_OK = 0,
     HPXFFT_ERR_INVALID_ARG = 1,      /* std::invalid_argument in the reference (bad plan flag) */
-    HPXFFT_ERR_UNSUPPORTED_SIZE = 2, /* odd ny, a prime factor above 13, too long a row */
+    HPXFFT_ERR_UNSUPPORTED_SIZE = 2, /* odd ny, or a size outside the limits of hpxfft_plan_create */
     HPXFFT_ERR_ALLOC = 3,            /* device or pinned allocation failed */
     HPXFFT_ERR_CUDA = 4,             /* a CUDA runtime call failed */
     HPXFFT_ERR_TIMEOUT = 5,          /* a bounded device-side wait gave up */
@@ -74,13 +74,20 @@ typedef struct hpxfft_plan3d_s *hpxfft_plan3d;
  * Measurements "cached_plan", "autotune_candidates", "autotune_ms_<i>",
  * "autotune_best_ms" and "choice_*" describe the search.
  * Allocates the twiddle tables and no data buffer.
- * Sizes: ny even; ny/2 (the row's complex length) and n_row without a prime
- * factor above 13.  A row runs on a cluster of C in {1, 2, 4} CTAs of at
+ * Sizes: ny even, any n_row (as FFTW takes them); batch <= 65535.  The
+ * direct kernels take ny/2 (the row's complex length) and n_row without a
+ * prime factor above 13: a row on a cluster of C in {1, 2, 4} CTAs of at
  * most 8192 complex values each, a column on C in {1, 2, 4, 8, 16} CTAs of
- * at most 4096 (FP64) or 8192 (FP32) each; C > 1 needs the length
- * divisible by C^2.  So ny <= 65536 and n_row <= 65536 (FP64) or 131072
- * (FP32).  batch <= 65535.  Other sizes return HPXFFT_ERR_UNSUPPORTED_SIZE
- * before any device call.
+ * at most 4096 (FP64) or 8192 (FP32) each, C > 1 needing the length
+ * divisible by C^2, and power-of-two n_row up to 2^24 (FP64) or 2^25
+ * (FP32) through the two-kernel column pass.  Other lengths take
+ * Bluestein's convolution through power-of-two column plans, and rows
+ * outside the direct kernels run as a column pass on a transposed copy
+ * (n_row <= 2^21 there); measurements "bluestein_rows", "bluestein_columns"
+ * (the convolution length, 0 when unused) and "transposed_rows" say which.
+ * Split-BF16 (n_row a power of two in [1024, 65536]) keeps the direct
+ * kernels' sizes.  Sizes outside all of these return
+ * HPXFFT_ERR_UNSUPPORTED_SIZE before any device call.
  * Replaces: hpxfft::shared::loop::initialize (core/src/shared/loop.cpp:158-189)
  * and fftw_adapter::{r2c_1d,c2c_1d}::plan (core/src/util/adapter_fftw.cpp:6-10,24-30),
  * string_to_fftw_plan_flag (core/include/hpxfft/util/adapter_fftw.hpp:22-44). */
