@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "bluestein.cuh"
+#include "cplx.cuh"
 
 namespace hpxfft_gpu {
 
@@ -142,23 +143,56 @@ cudaError_t bluestein_tables(size_t L, size_t M, int fmt, void **chirp, void **k
     return e;
 }
 
-cudaError_t split_table(size_t h, bool f32, void **w)
+cudaError_t split_table(size_t h, int fmt, void **w)
 {
     std::vector<double> v(2 * (h + 1));
     for (size_t k = 0; k <= h; ++k) cis(k, 2 * h, v[2 * k], v[2 * k + 1]);
-    return upload(v, f32 ? kTabF32 : kTabF64, w);
+    return upload(v, fmt, w);
 }
 
 // ---------------------------------------------------------------- kernels
 
-template <class V>
-__device__ __forceinline__ V vmul(V a, V b)
-{
-    V r;
-    r.x = a.x * b.x - a.y * b.y;
-    r.y = a.x * b.y + a.y * b.x;
-    return r;
-}
+// Storage and arithmetic of the three modes: FP32; FP64 on the DFMA pipe;
+// FP64 storage with float-float arithmetic on the FP32 pipes (the FP64
+// pipe runs 1/67 of the FP32 rate on this part).  Float-float values are
+// scaled by 2^-E, E the larger exponent of the doubles they came from
+// (integer-only conversions, exact scaling).
+template <int MODE>
+struct Elem;
+template <>
+struct Elem<kTabF32> {
+    using V = float2;
+    using T = float;
+    static __device__ __forceinline__ int exp_of(V) { return 0; }
+    static __device__ __forceinline__ cpx<T> in(V v, int) { return cpx<T>{v.x, v.y}; }
+    static __device__ __forceinline__ V out(cpx<T> v, int) { return make_float2(v.re, v.im); }
+};
+template <>
+struct Elem<kTabF64> {
+    using V = double2;
+    using T = double;
+    static __device__ __forceinline__ int exp_of(V) { return 0; }
+    static __device__ __forceinline__ cpx<T> in(V v, int) { return cpx<T>{v.x, v.y}; }
+    static __device__ __forceinline__ V out(cpx<T> v, int) { return make_double2(v.re, v.im); }
+};
+template <>
+struct Elem<kTabFF> {
+    using V = double2;
+    using T = ff;
+    static __device__ __forceinline__ int exp_of(V v)
+    {
+        const int e = max(dbl_biased_exp(v.x), dbl_biased_exp(v.y));
+        return (e == 0 || e == 0x7ff) ? 0 : e - 1023;
+    }
+    static __device__ __forceinline__ cpx<T> in(V v, int E)
+    {
+        return cpx<T>{ff_from_double(v.x, E), ff_from_double(v.y, E)};
+    }
+    static __device__ __forceinline__ V out(cpx<T> v, int E)
+    {
+        return make_double2(ff_to_double(renorm(v.re), E), ff_to_double(renorm(v.im), E));
+    }
+};
 
 template <class V>
 __device__ __forceinline__ V vzero()
@@ -169,26 +203,36 @@ __device__ __forceinline__ V vzero()
     return r;
 }
 
-template <class V>
-__device__ __forceinline__ V tab_at(const V *tab, long long i, int conj)
+template <class T>
+__device__ __forceinline__ cpx<T> tab_at(const cpx<T> *tab, long long i, int conj)
 {
-    V f = tab[i];
-    if (conj) f.y = -f.y;
-    return f;
+    const cpx<T> f = tab[i];
+    return conj ? cconj(f) : f;
 }
 
-template <class V>
-__global__ void __launch_bounds__(256) scale_rows_kernel(const V *in, long long in_rs, long long in_bs, V *out,
-                                                         long long out_rs, long long out_bs, const V *tab, int conj,
-                                                         long long rows_in, long long rows_out, long long ncols)
+// f v in the mode's arithmetic, back to storage
+template <int MODE>
+__device__ __forceinline__ typename Elem<MODE>::V scaled(typename Elem<MODE>::V v, cpx<typename Elem<MODE>::T> f)
 {
+    using E_ = Elem<MODE>;
+    const int E = E_::exp_of(v);
+    return E_::out(cmul(E_::in(v, E), f), E);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256)
+    scale_rows_kernel(const typename Elem<MODE>::V *in, long long in_rs, long long in_bs, typename Elem<MODE>::V *out,
+                      long long out_rs, long long out_bs, const cpx<typename Elem<MODE>::T> *tab, int conj,
+                      long long rows_in, long long rows_out, long long ncols)
+{
+    using V = typename Elem<MODE>::V;
     const long long b = blockIdx.z;
     const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= ncols) return;
     for (long long r = (long long)blockIdx.y * blockDim.y + threadIdx.y; r < rows_out;
          r += (long long)gridDim.y * blockDim.y) {
         V v = vzero<V>();
-        if (r < rows_in) v = vmul(in[b * in_bs + r * in_rs + j], tab_at(tab, r, conj));
+        if (r < rows_in) v = scaled<MODE>(in[b * in_bs + r * in_rs + j], tab_at(tab, r, conj));
         out[b * out_bs + r * out_rs + j] = v;
     }
 }
@@ -196,12 +240,14 @@ __global__ void __launch_bounds__(256) scale_rows_kernel(const V *in, long long 
 // 32 x 32 tiles through shared memory (odd row pitch: no bank conflicts for
 // 8- or 16-byte elements), 256 threads, 4 elements per thread each way;
 // blockIdx.x = row tile * col_tiles + col tile of the destination
-template <class V>
+template <int MODE>
 __global__ void __launch_bounds__(256)
-    transpose_scaled_kernel(const V *src, long long s_rs, long long s_bs, long long src_rows, long long src_cols, V *dst,
-                            long long d_rs, long long d_bs, long long dst_rows, long long dst_cols, unsigned col_tiles,
-                            const V *tab, int tab_on_col, int conj)
+    transpose_scaled_kernel(const typename Elem<MODE>::V *src, long long s_rs, long long s_bs, long long src_rows,
+                            long long src_cols, typename Elem<MODE>::V *dst, long long d_rs, long long d_bs,
+                            long long dst_rows, long long dst_cols, unsigned col_tiles,
+                            const cpx<typename Elem<MODE>::T> *tab, int tab_on_col, int conj)
 {
+    using V = typename Elem<MODE>::V;
     __shared__ V tile[32][33];
     const long long r0 = (long long)(blockIdx.x / col_tiles) * 32, c0 = (long long)(blockIdx.x % col_tiles) * 32;
     const long long b = blockIdx.z;
@@ -212,7 +258,7 @@ __global__ void __launch_bounds__(256)
         V v = vzero<V>();
         if (c < src_rows && r < src_cols) {
             v = src[b * s_bs + c * s_rs + r];
-            if (tab) v = vmul(v, tab_at(tab, tab_on_col ? c : r, conj));
+            if (tab) v = scaled<MODE>(v, tab_at(tab, tab_on_col ? c : r, conj));
         }
         tile[ty + 8 * q][tx] = v;
     }
@@ -225,61 +271,65 @@ __global__ void __launch_bounds__(256)
 }
 
 // blockIdx.x = k tile * i_tiles + i tile
-template <class V>
-__global__ void __launch_bounds__(256) r2c_split_kernel(const V *t, long long t_rs, long long t_bs, long long h,
-                                                        const V *chirp, const V *w, V *out, long long o_rs,
-                                                        long long o_bs, long long nrows, unsigned i_tiles)
+template <int MODE>
+__global__ void __launch_bounds__(256)
+    r2c_split_kernel(const typename Elem<MODE>::V *t, long long t_rs, long long t_bs, long long h,
+                     const cpx<typename Elem<MODE>::T> *chirp, const cpx<typename Elem<MODE>::T> *w,
+                     typename Elem<MODE>::V *out, long long o_rs, long long o_bs, long long nrows, unsigned i_tiles)
 {
-    using R = decltype(V{}.x);
-    __shared__ V za[32][33], zb[32][33];
+    using E_ = Elem<MODE>;
+    using V = typename E_::V;
+    using T = typename E_::T;
+    __shared__ cpx<T> za[32][33], zb[32][33];
+    __shared__ int ze[32][33];
     const long long k0 = (long long)(blockIdx.x / i_tiles) * 32, i0 = (long long)(blockIdx.x % i_tiles) * 32;
     const long long b = blockIdx.z;
     const int tx = threadIdx.x, ty = threadIdx.y;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const long long k = k0 + ty + 8 * q, i = i0 + tx;
-        V a = vzero<V>(), c = vzero<V>();
-        if (k <= h && i < nrows) {
-            const long long ka = k == h ? 0 : k, kb = k == 0 ? 0 : h - k;
-            a = t[b * t_bs + ka * t_rs + i];
-            c = t[b * t_bs + kb * t_rs + i];
-            if (chirp) {
-                a = vmul(a, chirp[ka]);
-                c = vmul(c, chirp[kb]);
-            }
+        const bool live = k <= h && i < nrows;
+        const long long ka = k == h ? 0 : k, kb = k == 0 ? 0 : h - k;
+        V a2 = vzero<V>(), c2 = vzero<V>();
+        if (live) {
+            a2 = t[b * t_bs + ka * t_rs + i];
+            c2 = t[b * t_bs + kb * t_rs + i];
+        }
+        const int E = max(E_::exp_of(a2), E_::exp_of(c2));  // one scale for the pair
+        cpx<T> a = E_::in(a2, E), c = E_::in(c2, E);
+        if (chirp && live) {
+            a = cmul(a, chirp[ka]);
+            c = cmul(c, chirp[kb]);
         }
         za[ty + 8 * q][tx] = a;
         zb[ty + 8 * q][tx] = c;
+        ze[ty + 8 * q][tx] = E;
     }
     __syncthreads();
-    const R half = (R)0.5;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const long long i = i0 + ty + 8 * q, k = k0 + tx;
         if (k <= h && i < nrows) {
-            const V a = za[tx][ty + 8 * q], c = zb[tx][ty + 8 * q];  // Z[k], Z[h-k]
-            V e, o;
-            e.x = (a.x + c.x) * half;  // (Z[k] + conj Z[h-k]) / 2
-            e.y = (a.y - c.y) * half;
-            o.x = (a.x - c.x) * half;  // (Z[k] - conj Z[h-k]) / 2
-            o.y = (a.y + c.y) * half;
-            const V wo = vmul(w[k], o);
-            V x;
-            x.x = e.x + wo.y;  // e - i wo
-            x.y = e.y - wo.x;
-            out[b * o_bs + i * o_rs + k] = x;
+            const cpx<T> a = za[tx][ty + 8 * q], c = cconj(zb[tx][ty + 8 * q]);  // Z[k], conj Z[h-k]
+            const cpx<T> e = chalf(a + c), o = chalf(a - c);
+            const cpx<T> wo = cmul(w[k], o);
+            const cpx<T> x{e.re + wo.im, e.im - wo.re};  // e - i wo
+            out[b * o_bs + i * o_rs + k] = E_::out(x, ze[tx][ty + 8 * q]);
         }
     }
 }
 
 // blockIdx.x = k tile * i_tiles + i tile
-template <class V>
+template <int MODE>
 __global__ void __launch_bounds__(256)
-    c2r_merge_kernel(const V *in, long long i_rs, long long i_bs, long long nrows, long long h, const V *chirp,
-                     const V *w, int adjoint, V *t, long long t_rs, long long t_bs, long long t_rows, long long t_cols,
+    c2r_merge_kernel(const typename Elem<MODE>::V *in, long long i_rs, long long i_bs, long long nrows, long long h,
+                     const cpx<typename Elem<MODE>::T> *chirp, const cpx<typename Elem<MODE>::T> *w, int adjoint,
+                     typename Elem<MODE>::V *t, long long t_rs, long long t_bs, long long t_rows, long long t_cols,
                      unsigned i_tiles)
 {
-    using R = decltype(V{}.x);
+    using E_ = Elem<MODE>;
+    using V = typename E_::V;
+    using T = typename E_::T;
     __shared__ V tile[32][33];
     const long long k0 = (long long)(blockIdx.x / i_tiles) * 32, i0 = (long long)(blockIdx.x % i_tiles) * 32;
     const long long b = blockIdx.z;
@@ -287,29 +337,27 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const long long k = k0 + tx, i = i0 + ty + 8 * q;
-        V z = vzero<V>();
+        V zo = vzero<V>();
         if (k < h && i < nrows) {
-            V a = in[b * i_bs + i * i_rs + k], c = in[b * i_bs + i * i_rs + (h - k)];
+            V a2 = in[b * i_bs + i * i_rs + k], c2 = in[b * i_bs + i * i_rs + (h - k)];
             if (k == 0) {  // X[0] and X[h]: imaginary parts ignored
-                a.y = 0;
-                c.y = 0;
-            } else if (adjoint) {  // interior bins halved
-                a.x *= (R)0.5;
-                a.y *= (R)0.5;
-                c.x *= (R)0.5;
-                c.y *= (R)0.5;
+                a2.y = 0;
+                c2.y = 0;
             }
-            V s, d;
-            s.x = a.x + c.x;  // X[k] + conj X[h-k]
-            s.y = a.y - c.y;
-            d.x = a.x - c.x;  // X[k] - conj X[h-k]
-            d.y = a.y + c.y;
-            const V wd = vmul(tab_at(w, k, 1), d);
-            z.x = s.x - wd.y;  // s + i wd
-            z.y = s.y + wd.x;
-            if (chirp) z = vmul(z, tab_at(chirp, k, 1));
+            const int E = max(E_::exp_of(a2), E_::exp_of(c2));
+            cpx<T> a = E_::in(a2, E), c = E_::in(c2, E);
+            if (adjoint && k > 0) {  // interior bins halved
+                a = chalf(a);
+                c = chalf(c);
+            }
+            c = cconj(c);
+            const cpx<T> s = a + c, d = a - c;  // X[k] +- conj X[h-k]
+            const cpx<T> wd = cmul(tab_at(w, k, 1), d);
+            cpx<T> z{s.re - wd.im, s.im + wd.re};  // s + i wd
+            if (chirp) z = cmul(z, tab_at(chirp, k, 1));
+            zo = E_::out(z, E);
         }
-        tile[ty + 8 * q][tx] = z;  // [i][k]
+        tile[ty + 8 * q][tx] = zo;  // [i][k]
     }
     __syncthreads();
 #pragma unroll
@@ -323,7 +371,12 @@ __global__ void __launch_bounds__(256)
 
 static long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
 
-cudaError_t scale_rows(bool f32, const void *in, long long in_rs, long long in_bs, void *out, long long out_rs,
+template <int MODE>
+using VT = typename Elem<MODE>::V;
+template <int MODE>
+using CT = cpx<typename Elem<MODE>::T>;
+
+cudaError_t scale_rows(int mode, const void *in, long long in_rs, long long in_bs, void *out, long long out_rs,
                        long long out_bs, const void *tab, int conj, long long rows_in, long long rows_out,
                        long long ncols, int batch, cudaStream_t st)
 {
@@ -336,13 +389,16 @@ cudaError_t scale_rows(bool f32, const void *in, long long in_rs, long long in_b
     if (gy > 65535) gy = 65535;
     if (gx > 0x7fffffffLL || batch > 65535) return cudaErrorInvalidValue;
     const dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)batch), block(bx, by);
-    if (f32)
-        scale_rows_kernel<float2><<<grid, block, 0, st>>>((const float2 *)in, in_rs, in_bs, (float2 *)out, out_rs,
-                                                          out_bs, (const float2 *)tab, conj, rows_in, rows_out, ncols);
-    else
-        scale_rows_kernel<double2><<<grid, block, 0, st>>>((const double2 *)in, in_rs, in_bs, (double2 *)out, out_rs,
-                                                           out_bs, (const double2 *)tab, conj, rows_in, rows_out,
-                                                           ncols);
+#define HPXFFT_M(MODE)                                                                                           \
+    scale_rows_kernel<MODE><<<grid, block, 0, st>>>((const VT<MODE> *)in, in_rs, in_bs, (VT<MODE> *)out, out_rs, \
+                                                    out_bs, (const CT<MODE> *)tab, conj, rows_in, rows_out, ncols)
+    switch (mode) {
+    case kTabF32: HPXFFT_M(kTabF32); break;
+    case kTabF64: HPXFFT_M(kTabF64); break;
+    case kTabFF: HPXFFT_M(kTabFF); break;
+    default: return cudaErrorInvalidValue;
+    }
+#undef HPXFFT_M
     return cudaGetLastError();
 }
 
@@ -356,7 +412,7 @@ static bool tile_grid(long long rows, long long cols, int batch, dim3 &grid, uns
     return true;
 }
 
-cudaError_t transpose_scaled(bool f32, const void *src, long long s_rs, long long s_bs, long long src_rows,
+cudaError_t transpose_scaled(int mode, const void *src, long long s_rs, long long s_bs, long long src_rows,
                              long long src_cols, void *dst, long long d_rs, long long d_bs, long long dst_rows,
                              long long dst_cols, const void *tab, int tab_on_col, int conj, int batch,
                              cudaStream_t st)
@@ -366,18 +422,21 @@ cudaError_t transpose_scaled(bool f32, const void *src, long long s_rs, long lon
     unsigned ct = 0;
     if (!tile_grid(dst_rows, dst_cols, batch, grid, ct)) return cudaErrorInvalidValue;
     const dim3 block(32, 8);
-    if (f32)
-        transpose_scaled_kernel<float2><<<grid, block, 0, st>>>((const float2 *)src, s_rs, s_bs, src_rows, src_cols,
-                                                                (float2 *)dst, d_rs, d_bs, dst_rows, dst_cols, ct,
-                                                                (const float2 *)tab, tab_on_col, conj);
-    else
-        transpose_scaled_kernel<double2><<<grid, block, 0, st>>>((const double2 *)src, s_rs, s_bs, src_rows,
-                                                                 src_cols, (double2 *)dst, d_rs, d_bs, dst_rows,
-                                                                 dst_cols, ct, (const double2 *)tab, tab_on_col, conj);
+#define HPXFFT_M(MODE)                                                                                    \
+    transpose_scaled_kernel<MODE><<<grid, block, 0, st>>>((const VT<MODE> *)src, s_rs, s_bs, src_rows,    \
+                                                          src_cols, (VT<MODE> *)dst, d_rs, d_bs, dst_rows, \
+                                                          dst_cols, ct, (const CT<MODE> *)tab, tab_on_col, conj)
+    switch (mode) {
+    case kTabF32: HPXFFT_M(kTabF32); break;
+    case kTabF64: HPXFFT_M(kTabF64); break;
+    case kTabFF: HPXFFT_M(kTabFF); break;
+    default: return cudaErrorInvalidValue;
+    }
+#undef HPXFFT_M
     return cudaGetLastError();
 }
 
-cudaError_t r2c_split(bool f32, const void *t, long long t_rs, long long t_bs, long long h, const void *chirp,
+cudaError_t r2c_split(int mode, const void *t, long long t_rs, long long t_bs, long long h, const void *chirp,
                       const void *w, void *out, long long o_rs, long long o_bs, long long nrows, int batch,
                       cudaStream_t st)
 {
@@ -386,16 +445,20 @@ cudaError_t r2c_split(bool f32, const void *t, long long t_rs, long long t_bs, l
     unsigned it = 0;
     if (!tile_grid(h + 1, nrows, batch, grid, it)) return cudaErrorInvalidValue;
     const dim3 block(32, 8);
-    if (f32)
-        r2c_split_kernel<float2><<<grid, block, 0, st>>>((const float2 *)t, t_rs, t_bs, h, (const float2 *)chirp,
-                                                         (const float2 *)w, (float2 *)out, o_rs, o_bs, nrows, it);
-    else
-        r2c_split_kernel<double2><<<grid, block, 0, st>>>((const double2 *)t, t_rs, t_bs, h, (const double2 *)chirp,
-                                                          (const double2 *)w, (double2 *)out, o_rs, o_bs, nrows, it);
+#define HPXFFT_M(MODE)                                                                                          \
+    r2c_split_kernel<MODE><<<grid, block, 0, st>>>((const VT<MODE> *)t, t_rs, t_bs, h, (const CT<MODE> *)chirp, \
+                                                   (const CT<MODE> *)w, (VT<MODE> *)out, o_rs, o_bs, nrows, it)
+    switch (mode) {
+    case kTabF32: HPXFFT_M(kTabF32); break;
+    case kTabF64: HPXFFT_M(kTabF64); break;
+    case kTabFF: HPXFFT_M(kTabFF); break;
+    default: return cudaErrorInvalidValue;
+    }
+#undef HPXFFT_M
     return cudaGetLastError();
 }
 
-cudaError_t c2r_merge(bool f32, const void *in, long long i_rs, long long i_bs, long long nrows, long long h,
+cudaError_t c2r_merge(int mode, const void *in, long long i_rs, long long i_bs, long long nrows, long long h,
                       const void *chirp, const void *w, int adjoint, void *t, long long t_rs, long long t_bs,
                       long long t_rows, long long t_cols, int batch, cudaStream_t st)
 {
@@ -404,14 +467,17 @@ cudaError_t c2r_merge(bool f32, const void *in, long long i_rs, long long i_bs, 
     unsigned it = 0;
     if (!tile_grid(t_rows, t_cols, batch, grid, it)) return cudaErrorInvalidValue;
     const dim3 block(32, 8);
-    if (f32)
-        c2r_merge_kernel<float2><<<grid, block, 0, st>>>((const float2 *)in, i_rs, i_bs, nrows, h,
-                                                         (const float2 *)chirp, (const float2 *)w, adjoint,
-                                                         (float2 *)t, t_rs, t_bs, t_rows, t_cols, it);
-    else
-        c2r_merge_kernel<double2><<<grid, block, 0, st>>>((const double2 *)in, i_rs, i_bs, nrows, h,
-                                                          (const double2 *)chirp, (const double2 *)w, adjoint,
-                                                          (double2 *)t, t_rs, t_bs, t_rows, t_cols, it);
+#define HPXFFT_M(MODE)                                                                                         \
+    c2r_merge_kernel<MODE><<<grid, block, 0, st>>>((const VT<MODE> *)in, i_rs, i_bs, nrows, h,                 \
+                                                   (const CT<MODE> *)chirp, (const CT<MODE> *)w, adjoint,     \
+                                                   (VT<MODE> *)t, t_rs, t_bs, t_rows, t_cols, it)
+    switch (mode) {
+    case kTabF32: HPXFFT_M(kTabF32); break;
+    case kTabF64: HPXFFT_M(kTabF64); break;
+    case kTabFF: HPXFFT_M(kTabFF); break;
+    default: return cudaErrorInvalidValue;
+    }
+#undef HPXFFT_M
     return cudaGetLastError();
 }
 

@@ -21,8 +21,11 @@
 //     scratch array, the column kernels transform them, and the r2c split
 //     (the row kernel's post-processing) runs while transposing back.
 //
-// Every kernel here is an HBM-bound elementwise or 32 x 32 tiled-transpose
-// pass; arithmetic in the storage type (FP32, or FP64 for the FP64 plans).
+// Every kernel here is an elementwise or 32 x 32 tiled-transpose pass in one
+// of three modes (TableFormat): FP32; FP64 on the DFMA pipe (the DFMA
+// plan); FP64 storage with float-float arithmetic (the FP64 plan: the FP64
+// pipe runs 1/67 of the FP32 rate on this part).  A plan's tables are in
+// its mode's format, which is also the column steps' compute type.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -33,9 +36,8 @@ namespace hpxfft_gpu {
 // Smallest power of two >= 2 L - 1: the convolution length for length L.
 size_t bluestein_length(size_t L);
 
-// Element formats of the device tables: FP32 or FP64 complex (the storage
-// types, for the kernels below), float-float complex (hi, lo per part: the
-// compute type of the float-float column steps, which apply the factors).
+// Arithmetic modes and table formats: FP32 complex, FP64 complex,
+// float-float complex (hi, lo per part).
 enum TableFormat { kTabF32 = 0, kTabF64 = 1, kTabFF = 2 };
 
 // Device tables for length L, convolution length M:
@@ -45,12 +47,12 @@ cudaError_t bluestein_tables(size_t L, size_t M, int fmt, void **chirp, void **k
 
 // Device table w[k] = W_2h^k = exp(-i pi k / h), k = 0..h (the r2c split of
 // rows of 2h reals).  Allocates; the caller frees.
-cudaError_t split_table(size_t h, bool f32, void **w);
+cudaError_t split_table(size_t h, int fmt, void **w);
 
 // out[b][r][j] = f(r) in[b][r][j] for r < rows_in, 0 for rows_in <= r < rows_out
 // (j < ncols); f(r) = tab[r], conjugated when conj.  Strides in complex
 // elements; `in` may be `out`.
-cudaError_t scale_rows(bool f32, const void *in, long long in_rs, long long in_bs, void *out, long long out_rs,
+cudaError_t scale_rows(int mode, const void *in, long long in_rs, long long in_bs, void *out, long long out_rs,
                        long long out_bs, const void *tab, int conj, long long rows_in, long long rows_out,
                        long long ncols, int batch, cudaStream_t st);
 
@@ -58,7 +60,7 @@ cudaError_t scale_rows(bool f32, const void *in, long long in_rs, long long in_b
 // (r < dst_rows, c < dst_cols); f = tab[r] (tab_on_col 0) or tab[c]
 // (tab_on_col 1), conjugated when conj, or 1 when tab is null.  `src` and
 // `dst` must not overlap.
-cudaError_t transpose_scaled(bool f32, const void *src, long long s_rs, long long s_bs, long long src_rows,
+cudaError_t transpose_scaled(int mode, const void *src, long long s_rs, long long s_bs, long long src_rows,
                              long long src_cols, void *dst, long long d_rs, long long d_bs, long long dst_rows,
                              long long dst_cols, const void *tab, int tab_on_col, int conj, int batch,
                              cudaStream_t st);
@@ -68,7 +70,7 @@ cudaError_t transpose_scaled(bool f32, const void *src, long long s_rs, long lon
 // packed rows; row i of `out` gets, for k = 0..h,
 //   X[k] = (Z[k] + conj Z[h-k]) / 2 - (i / 2) W_2h^k (Z[k] - conj Z[h-k])
 // (indices mod h), the same split the row kernel applies.
-cudaError_t r2c_split(bool f32, const void *t, long long t_rs, long long t_bs, long long h, const void *chirp,
+cudaError_t r2c_split(int mode, const void *t, long long t_rs, long long t_bs, long long h, const void *chirp,
                       const void *w, void *out, long long o_rs, long long o_bs, long long nrows, int batch,
                       cudaStream_t st);
 
@@ -79,7 +81,7 @@ cudaError_t r2c_split(bool f32, const void *t, long long t_rs, long long t_bs, l
 // Im X[0] and Im X[h] taken as zero, the interior bins halved when adjoint,
 // f = conj chirp[k] (or 1 when chirp is null).  The inverse DFT of Z gives
 // the packed rows, as in the row kernel's c2r.
-cudaError_t c2r_merge(bool f32, const void *in, long long i_rs, long long i_bs, long long nrows, long long h,
+cudaError_t c2r_merge(int mode, const void *in, long long i_rs, long long i_bs, long long nrows, long long h,
                       const void *chirp, const void *w, int adjoint, void *t, long long t_rs, long long t_bs,
                       long long t_rows, long long t_cols, int batch, cudaStream_t st);
 

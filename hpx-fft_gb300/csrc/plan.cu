@@ -77,14 +77,13 @@ struct AltAxis {
     size_t L = 0, M = 0;
     size_t width = 0;
     hpxfft_plan sub = nullptr;
-    void *chirp = nullptr;   // L entries exp(-i pi n^2 / L) (storage type)
+    // tables in the plan's arithmetic (alt_mode: float-float pairs for the
+    // FP64 plan, the column steps' compute type)
+    void *chirp = nullptr;   // L entries exp(-i pi n^2 / L)
     void *kernel = nullptr;  // M entries: DFT_M of the conjugate chirp, over M
     void *wtab = nullptr;    // rows: W_2L^k, k = 0..L
-    // the same two tables in the column steps' compute type (float-float
-    // pairs for the FP64 plan, the same arrays for FP32): the steps apply
-    // them while loading and storing when the sub-plan takes the two-kernel
-    // pass (fused)
-    void *chirp_c = nullptr, *kernel_c = nullptr;
+    // the column steps apply chirp and kernel while loading and storing
+    // (the sub-plan takes the two-kernel pass)
     bool fused = false;
 };
 
@@ -160,6 +159,13 @@ namespace hpxfft_gpu {
 static bool f32_storage(int prec) { return prec == HPXFFT_PREC_F32 || prec == HPXFFT_PREC_BF16X3; }
 
 static int max_elems_for(int prec) { return f32_storage(prec) ? 8192 : 4096; }
+
+// arithmetic of the Bluestein / transposing kernels and format of their
+// tables: FP32, float-float on FP64 storage (the FP64 plan), DFMA FP64
+static int alt_mode(int prec)
+{
+    return f32_storage(prec) ? kTabF32 : prec == HPXFFT_PREC_F64 ? kTabFF : kTabF64;
+}
 
 static int threads_for(int nel)
 {
@@ -588,16 +594,16 @@ static cudaError_t run_steps_with(hpxfft_plan_s &q, const void *in, long long in
 template <class A>
 static cudaError_t alt_convolve(hpxfft_plan_s &p, AltAxis &a, void *scr, int dir)
 {
-    const bool f32 = f32_storage(p.prec);
+    const int mode = alt_mode(p.prec);
     const long long w = (long long)a.width, bs = (long long)(a.M * a.width);
     const int M = (int)a.M, conj = dir > 0;
     if (a.fused) {
-        cudaError_t e = run_steps_with<A>(*a.sub, scr, bs, scr, bs, -1, nullptr, 0, a.kernel_c, M, conj);
+        cudaError_t e = run_steps_with<A>(*a.sub, scr, bs, scr, bs, -1, nullptr, 0, a.kernel, M, conj);
         return e == cudaSuccess ? run_steps_with<A>(*a.sub, scr, bs, scr, bs, +1, nullptr, 0, nullptr, 0, 0) : e;
     }
     cudaError_t e = run_columns<A>(*a.sub, scr, -1, scr);
     if (e == cudaSuccess)
-        e = scale_rows(f32, scr, w, bs, scr, w, bs, a.kernel, conj, (long long)a.M, (long long)a.M, w, (int)p.batch,
+        e = scale_rows(mode, scr, w, bs, scr, w, bs, a.kernel, conj, (long long)a.M, (long long)a.M, w, (int)p.batch,
                        p.stream);
     if (e == cudaSuccess) e = run_columns<A>(*a.sub, scr, +1, scr);
     return e;
@@ -611,7 +617,7 @@ static cudaError_t run_alt_columns(hpxfft_plan_s &p, void *data, int dir)
 {
     AltAxis &a = p.alt_col;
     a.sub->stream = p.stream;
-    const bool f32 = f32_storage(p.prec);
+    const int mode = alt_mode(p.prec);
     const long long dcy = (long long)p.dcy, dbs = (long long)(p.nx * p.dcy), sbs = (long long)(a.M * a.width);
     const int conj = dir > 0, nb = (int)p.batch;
     if (a.fused) {
@@ -619,16 +625,16 @@ static cudaError_t run_alt_columns(hpxfft_plan_s &p, void *data, int dir)
         // step B's stores, the chirp back in the inverse's step B (which
         // writes only the nx rows of `data`)
         const int L = (int)p.nx, M = (int)a.M;
-        cudaError_t e = run_steps_with<A>(*a.sub, data, dbs, p.alt_buf, sbs, -1, a.chirp_c, L, a.kernel_c, M, conj);
+        cudaError_t e = run_steps_with<A>(*a.sub, data, dbs, p.alt_buf, sbs, -1, a.chirp, L, a.kernel, M, conj);
         return e == cudaSuccess
-                   ? run_steps_with<A>(*a.sub, p.alt_buf, sbs, data, dbs, +1, nullptr, 0, a.chirp_c, L, conj)
+                   ? run_steps_with<A>(*a.sub, p.alt_buf, sbs, data, dbs, +1, nullptr, 0, a.chirp, L, conj)
                    : e;
     }
-    cudaError_t e = scale_rows(f32, data, dcy, dbs, p.alt_buf, dcy, sbs, a.chirp, conj, (long long)p.nx,
+    cudaError_t e = scale_rows(mode, data, dcy, dbs, p.alt_buf, dcy, sbs, a.chirp, conj, (long long)p.nx,
                                (long long)a.M, dcy, nb, p.stream);
     if (e == cudaSuccess) e = alt_convolve<A>(p, a, p.alt_buf, dir);
     if (e == cudaSuccess)
-        e = scale_rows(f32, p.alt_buf, dcy, sbs, data, dcy, dbs, a.chirp, conj, (long long)p.nx, (long long)p.nx,
+        e = scale_rows(mode, p.alt_buf, dcy, sbs, data, dcy, dbs, a.chirp, conj, (long long)p.nx, (long long)p.nx,
                        dcy, nb, p.stream);
     return e;
 }
@@ -642,17 +648,17 @@ static cudaError_t run_alt_rows(hpxfft_plan_s &p, const void *in, void *out)
 {
     AltAxis &a = p.alt_row;
     a.sub->stream = p.stream;
-    const bool f32 = f32_storage(p.prec);
+    const int mode = alt_mode(p.prec);
     const long long dcy = (long long)p.dcy, dbs = (long long)(p.nx * p.dcy);
     const long long w = (long long)a.width, tbs = (long long)(a.M * a.width), h = (long long)p.M;
     const int nb = (int)p.batch;
     const void *chirp = a.bluestein ? a.chirp : nullptr;
-    cudaError_t e = transpose_scaled(f32, in, dcy, dbs, (long long)p.nx, h, p.alt_buf, w, tbs, (long long)a.M, w,
+    cudaError_t e = transpose_scaled(mode, in, dcy, dbs, (long long)p.nx, h, p.alt_buf, w, tbs, (long long)a.M, w,
                                      chirp, 0, 0, nb, p.stream);
     if (e == cudaSuccess)
         e = a.bluestein ? alt_convolve<A>(p, a, p.alt_buf, -1) : run_columns<A>(*a.sub, p.alt_buf, -1, p.alt_buf);
     if (e == cudaSuccess)
-        e = r2c_split(f32, p.alt_buf, w, tbs, h, chirp, a.wtab, out, dcy, dbs, (long long)p.nx, nb, p.stream);
+        e = r2c_split(mode, p.alt_buf, w, tbs, h, chirp, a.wtab, out, dcy, dbs, (long long)p.nx, nb, p.stream);
     return e;
 }
 
@@ -665,17 +671,17 @@ static cudaError_t run_alt_rows_c2r(hpxfft_plan_s &p, void *data, int adjoint)
 {
     AltAxis &a = p.alt_row;
     a.sub->stream = p.stream;
-    const bool f32 = f32_storage(p.prec);
+    const int mode = alt_mode(p.prec);
     const long long dcy = (long long)p.dcy, dbs = (long long)(p.nx * p.dcy);
     const long long w = (long long)a.width, tbs = (long long)(a.M * a.width), h = (long long)p.M;
     const int nb = (int)p.batch;
     const void *chirp = a.bluestein ? a.chirp : nullptr;
-    cudaError_t e = c2r_merge(f32, data, dcy, dbs, (long long)p.nx, h, chirp, a.wtab, adjoint, p.alt_buf, w, tbs,
+    cudaError_t e = c2r_merge(mode, data, dcy, dbs, (long long)p.nx, h, chirp, a.wtab, adjoint, p.alt_buf, w, tbs,
                               (long long)a.M, w, nb, p.stream);
     if (e == cudaSuccess)
         e = a.bluestein ? alt_convolve<A>(p, a, p.alt_buf, +1) : run_columns<A>(*a.sub, p.alt_buf, +1, p.alt_buf);
     if (e == cudaSuccess)
-        e = transpose_scaled(f32, p.alt_buf, w, tbs, h, (long long)p.nx, data, dcy, dbs, (long long)p.nx, dcy, chirp,
+        e = transpose_scaled(mode, p.alt_buf, w, tbs, h, (long long)p.nx, data, dcy, dbs, (long long)p.nx, dcy, chirp,
                              1, 1, nb, p.stream);
     return e;
 }
@@ -1052,20 +1058,12 @@ static int alt_sub_plan(hpxfft_plan_s &p, size_t len, size_t width, hpxfft_plan 
     return create_plan_with(sub, len, 2 * width, p.batch, p.prec, "estimate", kPlanColumns, PlanChoice{}, false);
 }
 
-// Bluestein tables for a.L, a.M in the storage type and, for the fused
-// path, in the column steps' compute type.
+// Bluestein tables for a.L, a.M in the plan's arithmetic.
 static int alt_tables(hpxfft_plan_s &p, AltAxis &a)
 {
-    const bool f32 = f32_storage(p.prec);
-    cudaError_t e = bluestein_tables(a.L, a.M, f32 ? kTabF32 : kTabF64, &a.chirp, &a.kernel);
+    cudaError_t e = bluestein_tables(a.L, a.M, alt_mode(p.prec), &a.chirp, &a.kernel);
     if (e != cudaSuccess) return cuda_fail(e, "Bluestein tables");
     a.fused = a.sub->col_two_step && !a.sub->tc_cols && p.prec != HPXFFT_PREC_F64_NATIVE;
-    if (f32) {
-        a.chirp_c = a.chirp;
-        a.kernel_c = a.kernel;
-    } else if (a.fused && (e = bluestein_tables(a.L, a.M, kTabFF, &a.chirp_c, &a.kernel_c)) != cudaSuccess) {
-        return cuda_fail(e, "Bluestein tables");
-    }
     return HPXFFT_OK;
 }
 
@@ -1074,7 +1072,6 @@ static int alt_tables(hpxfft_plan_s &p, AltAxis &a)
 static int setup_alt_rows(hpxfft_plan_s &p)
 {
     AltAxis &a = p.alt_row;
-    const bool f32 = f32_storage(p.prec);
     a.L = p.M;
     a.width = (std::max<size_t>(p.nx, 2) + 3) / 4 * 4;  // 64-byte rows of the scratch array start aligned
     int rc = alt_sub_plan(p, a.L, a.width, &a.sub);
@@ -1088,7 +1085,7 @@ static int setup_alt_rows(hpxfft_plan_s &p)
     } else {
         return rc;
     }
-    cudaError_t e = split_table(a.L, f32, &a.wtab);
+    cudaError_t e = split_table(a.L, alt_mode(p.prec), &a.wtab);
     return e == cudaSuccess ? HPXFFT_OK : cuda_fail(e, "split twiddles");
 }
 
@@ -1110,8 +1107,6 @@ static void free_alt(AltAxis &a)
         a.sub->stream = a.sub->own_stream;
         hpxfft_plan_destroy(a.sub);
     }
-    if (a.chirp_c != a.chirp) cudaFree(a.chirp_c);
-    if (a.kernel_c != a.kernel) cudaFree(a.kernel_c);
     cudaFree(a.chirp);
     cudaFree(a.kernel);
     cudaFree(a.wtab);
