@@ -457,6 +457,10 @@ struct RowArgs {
     int pairs_out;            // float-float r2c: store (hi, lo) pairs and one exponent per row
     int *exp_out;             // [batch][nrows] when pairs_out
     int prefetch;             // persistent r2c: prefetch the next row group into L2 (device input only)
+    // non-persistent r2c with one row group per CTA: prefetch into L2 the
+    // input of group blockIdx.x + prefetch_ahead (the CTA that takes this
+    // CTA's place once it is done: prefetch_ahead = CTAs resident at once); 0: none
+    int prefetch_ahead;
     // exponent slot of row r of batch item b (pairs_out): exp_out[b * exp_bstride + r]
     long long exp_bstride;
 };
@@ -854,6 +858,19 @@ __global__ void HPXFFT_BOUNDS(A, FL) row_r2c_kernel(RowArgs a)
             __syncthreads();  // shared memory is reused by the next group
         }
     } else {
+        if constexpr (C == 1) {
+            if (a.prefetch_ahead) {
+                using S = typename A::S;
+                const int log2W = FL > 0 ? FW : a.log2W;
+                const int next = (int)blockIdx.x + a.prefetch_ahead;
+                if (next < (int)gridDim.x) {
+                    const int r0 = next << log2W, nr = min(1 << log2W, a.nrows - r0);
+                    const S *src = reinterpret_cast<const S *>(a.in) + (long long)blockIdx.y * a.in_bstride +
+                                   (long long)r0 * a.in_stride;
+                    if (nr > 0) prefetch_l2(src, (long long)nr * a.in_stride * (long long)sizeof(S));
+                }
+            }
+        }
         row_r2c_body<A, C, FL, FW>(a, blockIdx.x / C, blockIdx.y);
     }
 }

@@ -149,6 +149,17 @@ static cudaError_t launch_persistent(K kernel, const Args &a, const LaunchShape 
     return launch_cluster(kernel, a, p, st);
 }
 
+// One row group per CTA: each CTA prefetches into L2 the group of the CTA
+// that will take its place (block + resident CTAs), so that CTA's
+// first-pass loads hit L2 (single-CTA shapes, device input only).
+template <class K>
+static cudaError_t launch_rows_ahead(K kernel, const RowArgs &a, const LaunchShape &s, int C, cudaStream_t st)
+{
+    RowArgs b = a;
+    b.prefetch_ahead = C == 1 && a.prefetch ? resident_ctas(kernel, s) : 0;
+    return launch_cluster(kernel, b, s, st);
+}
+
 template <class K>
 static cudaError_t set_attrs(K kernel, bool nonportable)
 {
@@ -211,7 +222,7 @@ cudaError_t RowLaunch<A>::r2c(const RowArgs &a, const LaunchShape &s, int FL, cu
 #define HPXFFT_X(L_, W_, C_)                                                                            \
     if (FL == L_ && a.log2W == W_ && s.cluster == C_)                                                   \
         return row_persistent<A>(C_, L_, W_) ? launch_persistent(row_r2c_kernel<A, C_, L_, W_>, a, s, st) \
-                       : launch_cluster(row_r2c_kernel<A, C_, L_, W_>, a, s, st);
+                                             : launch_rows_ahead(row_r2c_kernel<A, C_, L_, W_>, a, s, C_, st);
             if constexpr (sizeof(typename A::S) == 4) {
                 HPXFFT_ROW_FIXED_F32(HPXFFT_X)
             } else {
