@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP32 / batch / backward sections")
     ap.add_argument("--batch-only", action="store_true", help="only the uneven FP32 batch (profiling)")
+    ap.add_argument("--prime-only", action="store_true",
+                    help="only the prime-length transforms beside cuFFT (profiling; --nx/--ny set the size)")
     ap.add_argument("--batch-count", type=int, default=1024)
     ap.add_argument("--batch-flag", default="measure", choices=["estimate", "measure"])
     args = ap.parse_args()
@@ -608,12 +610,11 @@ def cufft_side(torch, stream, x64, nx, ny, steps, warm, oracle_ref, peak):
     return res
 
 
-def prime_sizes(torch, hpxfft, stream, steps, warm, peak):
+def prime_sizes(torch, hpxfft, stream, steps, warm, peak, nx=16381, ny=16382):
     """16381 x 16382 (16381 and ny/2 = 8191 prime): Bluestein's convolution
     on both passes, FP64 (float-float) and FP32, beside cuFFT on the same
     input.  The error reference is cuFFT's FP64 output (the oracle's O(p^2)
     radix-p step is too slow at this size); value uses the same 4 S bytes."""
-    nx, ny = 16381, 16382
     nc = 2 * (ny // 2 + 1)
     g = torch.Generator(device="cuda")
     g.manual_seed(16381)
@@ -754,12 +755,35 @@ def run_batch_only(args):
     return 0
 
 
+def run_prime_only(args):
+    """The prime-length section alone, one JSON line (profiling the
+    Bluestein path; --nx/--ny other than the 16384^2 default set the size)."""
+    import importlib.util
+
+    import torch
+
+    torch.cuda.set_device(0)
+    spec = importlib.util.spec_from_file_location("hpxfft_build", os.path.join(REPO, "hpx-fft_gb300", "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    b.build_all()
+    import hpxfft
+
+    peak, _ = measured_peak_hbm()
+    nx, ny = (args.nx, args.ny) if (args.nx, args.ny) != (16384, 16384) else (16381, 16382)
+    res = prime_sizes(torch, hpxfft, torch.cuda.current_stream(), args.steps, max(3, args.warmup), peak, nx, ny)
+    print(json.dumps(res), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.batch_only:
         return run_batch_only(args)
+    if args.prime_only:
+        return run_prime_only(args)
     return run_ours(args)
 
 
