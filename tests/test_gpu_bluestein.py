@@ -154,3 +154,26 @@ def test_plan_description_names_the_path(gpu_lib, cuda, tmp_path):
     text = path.read_text()
     assert "Bluestein, length 89 through 256" in text
     assert "Bluestein, length 97 through 256" in text
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_random_sizes_against_pocketfft(gpu_lib, cuda, prec):
+    """30 seeded random shapes, n_row in [1, 6000] and even ny in [2, 12000]
+    (smooth, prime and mixed lengths, so every path and the direct kernels
+    alternate), forward and c2r against numpy's pocketfft."""
+    rng = np.random.default_rng(40)
+    dt = np.float32 if prec == "f32" else np.float64
+    tol = TOL[prec]
+    for _ in range(30):
+        nx = int(rng.integers(1, 6001))
+        ny = 2 * int(rng.integers(1, 6001))
+        x = rng.uniform(-1, 1, (nx, ny))
+        if prec == "f32":
+            x = x.astype(np.float32).astype(np.float64)
+        with gpu_lib.Plan(nx, 2 * (ny // 2 + 1), 1, prec, "estimate") as plan:
+            X = run_device(cuda, plan, padded(x).astype(dt)).astype(np.float64)
+            back = run_device(cuda, plan, X.astype(dt), "c2r").astype(np.float64)
+        ref = np.fft.rfft2(x)
+        assert rel_l2(X.view(np.complex128), ref) <= tol, (prec, nx, ny)
+        assert rel_l2(back[:, :ny] / (nx * ny), x) <= 2 * tol, (prec, nx, ny)
+
