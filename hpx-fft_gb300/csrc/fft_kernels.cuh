@@ -1235,6 +1235,7 @@ struct ColStepArgs {
     // exponent exp_in[(r % exp_rmod) * exp_rmul + (col0 >> exp_cshift)]
     // (per-row exponents of the row kernel, or per-block ones of step A);
     // pairs_out stores pairs and exp_out[blockIdx.x + gridDim.x * batch]
+    // (from pair input or, in colstep_kernel, from double input)
     int pairs_in, pairs_out;
     const int *exp_in;
     int exp_rmod, exp_rmul, exp_cshift;
@@ -1249,8 +1250,8 @@ struct ColStepArgs {
     // input row r is multiplied by pre_tab[r] and rows r >= pre_rows read as
     // zero without a load; output row r is multiplied by post_tab[r] and
     // rows r >= post_rows are not written; both conjugated when tab_conj.
-    // Null: none.  Only colstep_kernel applies them (the launcher picks it
-    // whenever a table is given).
+    // Null: none.  colstep_kernel applies both, colstep_warp_kernel the
+    // output factors (the launcher routes input factors to colstep_kernel).
     const void *pre_tab, *post_tab;
     int pre_rows, post_rows;
     int tab_conj;
@@ -1365,7 +1366,28 @@ __global__ void HPXFFT_BOUNDS(A, FL) colstep_kernel(ColStepArgs a)
     else
         local_fft<T, DIR>(s, L, log2W, a.pp, tw, a.Ltab);
 
-    const bool pairs_out = pairs_in && a.pairs_out;
+    // pairs out: pair input keeps its block exponent; double input (one
+    // scale per column) takes the largest column exponent for the block and
+    // rescales the other columns to it (exact powers of two)
+    const bool pairs_out = A::kScaled && kFixed && a.pairs_out;
+    __shared__ float sFo[64];  // per-column factors to the block exponent
+    if constexpr (A::kScaled && kFixed) {
+        if (pairs_out && !pairs_in) {
+            __shared__ int sEo;
+            if (tid == 0) {
+                int m = kExpNone;
+                for (int w = 0; w < (1 << log2W); ++w) m = max(m, block_exp(sEc[w]));
+                sEo = m;
+            }
+            __syncthreads();
+            Eblk = sEo;
+            if (tid < (1 << log2W)) {
+                const int ew = block_exp(sEc[tid]);
+                sFo[tid] = ew == kExpNone || Eblk == kExpNone ? 0.0f : pow2_le0(ew - Eblk);
+            }
+            __syncthreads();
+        }
+    }
     if (pairs_out && tid == 0) a.exp_out[bx + (long long)a.grid_blocks * blockIdx.y] = Eblk;
     for (int t = t0; t < nel; t += nth) {
         const int w = t & wmask, k = t >> log2W, col = col0 + w;
@@ -1379,10 +1401,14 @@ __global__ void HPXFFT_BOUNDS(A, FL) colstep_kernel(ColStepArgs a)
             v = cmul(v, row_factor(post, orow, a.tab_conj));
         }
         S *o = out + orow * a.row_stride + 2 * (long long)col;
-        if (pairs_out)
+        if (pairs_out) {
+            if constexpr (A::kScaled) {
+                if (!pairs_in) v = cpx<T>{ff_scale_pow2(v.re, sFo[w]), ff_scale_pow2(v.im, sFo[w])};
+            }
             store_pair<A>(o, v);
-        else
+        } else {
             store_c<A>(o, v, E);
+        }
     }
 }
 
@@ -1444,7 +1470,8 @@ struct WarpLocalPasses {
     }
 };
 
-template <class A, int DIR, int FL, int FW>
+// RF: the instance that applies ColStepArgs' per-row output factors
+template <class A, int DIR, int FL, int FW, bool RF = false>
 __global__ void __launch_bounds__((FL << FW) / A::kEPTFixed, kFixedMinBlocks) colstep_warp_kernel(ColStepArgs a)
 {
     using T = typename A::T;
@@ -1514,6 +1541,11 @@ __global__ void __launch_bounds__((FL << FW) / A::kEPTFixed, kFixedMinBlocks) co
         if (col >= a.ncols) continue;
         cpx<T> v = s[w * CS + pidx(k)];
         if (a.post && g) v = cmul(v, twid<DIR>(tw, g * k));
+        if constexpr (RF) {  // per-row output factors (Bluestein)
+            const long long orow = out_row0 + (long long)a.out_step * k;
+            if (orow >= a.post_rows) continue;
+            v = cmul(v, row_factor(reinterpret_cast<const cpx<T> *>(a.post_tab), orow, a.tab_conj));
+        }
         S *o = out + (out_row0 + (long long)a.out_step * k) * a.row_stride + 2 * (long long)col;
         if (pairs_out)
             store_pair<A>(o, v);

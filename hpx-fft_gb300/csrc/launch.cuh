@@ -348,6 +348,7 @@ cudaError_t ColStepLaunch<A>::prepare()
         HPXFFT_TRY(set_attrs(colstep_direct_kernel<A, +1, L, W>, false));  \
     } else {                                                           \
         HPXFFT_TRY(set_attrs(colstep_warp_kernel<A, -1, L, W>, false));    \
+        HPXFFT_TRY(set_attrs(colstep_warp_kernel<A, -1, L, W, true>, false));  \
     }
         if constexpr (sizeof(typename A::S) == 4) {
             HPXFFT_COLSTEP_FIXED_F32(HPXFFT_X)
@@ -382,7 +383,7 @@ cudaError_t ColStepLaunch<A>::run(const ColStepArgs &a, int dir, const LaunchSha
         // -> 0.46 / 0.40 ms); float-float is arithmetic-bound and measured no
         // faster that way, so it keeps the staged kernel
         // per-row factors (Bluestein): the staged kernel, whose registers
-        // hold them without spilling
+        // hold them without spilling (the warp-local one takes output factors)
         const bool row_factors = a.pre_tab || a.post_tab;
         if constexpr (sizeof(typename A::S) == 4) {
             if (FL && !row_factors) {
@@ -397,12 +398,13 @@ cudaError_t ColStepLaunch<A>::run(const ColStepArgs &a, int dir, const LaunchSha
         }
         if constexpr (sizeof(typename A::S) == 8) {
             // float-float forward steps with pair input: warp-local passes
-            if (FL && a.pairs_in && a.warp_local && dir < 0 && !row_factors) {
+            if (FL && a.pairs_in && a.warp_local && dir < 0 && !a.pre_tab) {
 #define HPXFFT_X(L_, W_)                                                                              \
     if (FL == L_ && a.log2W == W_) {                                                                  \
         LaunchShape ws = s;                                                                           \
         ws.smem = (size_t)(1 << W_) * wl_col_stride(L_) * sizeof(cpx<typename A::T>);                 \
-        return launch_cluster(colstep_warp_kernel<A, -1, L_, W_>, a, ws, st);                         \
+        return a.post_tab ? launch_cluster(colstep_warp_kernel<A, -1, L_, W_, true>, a, ws, st)       \
+                          : launch_cluster(colstep_warp_kernel<A, -1, L_, W_>, a, ws, st);            \
     }
                 HPXFFT_COLSTEP_FIXED_FF(HPXFFT_X)
 #undef HPXFFT_X

@@ -85,6 +85,9 @@ struct AltAxis {
     // the column steps apply chirp and kernel while loading and storing
     // (the sub-plan takes the two-kernel pass)
     bool fused = false;
+    // float-float plans: steps A and B of the sub-plan exchange raw pairs
+    // with one exponent per step-A block (as the FP64 plan's own steps do)
+    int *exp_blocks = nullptr;
 };
 
 }  // namespace hpxfft_gpu
@@ -568,22 +571,35 @@ static cudaError_t run_columns(hpxfft_plan_s &p, void *data, int dir, void *dst)
 // their own, q's row stride), with per-row factors on step A's input
 // (rows past pre_rows read as zero) and on step B's output (rows past
 // post_rows not written).
+// With `exp` (float-float sub-plans), step A stores raw pairs and one
+// exponent per block into exp, and step B reads them.
 template <class A>
 static cudaError_t run_steps_with(hpxfft_plan_s &q, const void *in, long long in_bs, void *out, long long out_bs,
-                                  int dir, const void *pre, int pre_rows, const void *post, int post_rows, int conj)
+                                  int dir, const void *pre, int pre_rows, const void *post, int post_rows, int conj,
+                                  int *exp = nullptr)
 {
     ColStepArgs sa = colstep_args(q, 0, in, q.scratch);
     sa.in_bstride = in_bs;
     sa.pre_tab = pre;
     sa.pre_rows = pre_rows;
     sa.tab_conj = conj;
-    cudaError_t e = ColStepLaunch<A>::run(sa, dir, q.colA.shape, q.colA.FL, q.stream);
-    if (e != cudaSuccess) return e;
     ColStepArgs sb = colstep_args(q, 1, q.scratch, out);
     sb.out_bstride = out_bs;
     sb.post_tab = post;
     sb.post_rows = post_rows;
     sb.tab_conj = conj;
+    if (exp) {
+        sa.pairs_out = 1;
+        sa.exp_out = exp;
+        sb.pairs_in = 1;
+        sb.exp_in = exp;
+        sb.exp_rmod = q.N1;  // scratch row N1 g + m came from step A block (m, strip)
+        sb.exp_rmul = sa.strips;
+        sb.exp_cshift = q.colA.log2W;
+        sb.exp_in_bstride = (long long)q.colA.shape.grid.x;
+    }
+    cudaError_t e = ColStepLaunch<A>::run(sa, dir, q.colA.shape, q.colA.FL, q.stream);
+    if (e != cudaSuccess) return e;
     return ColStepLaunch<A>::run(sb, dir, q.colB.shape, q.colB.FL, q.stream);
 }
 
@@ -598,8 +614,10 @@ static cudaError_t alt_convolve(hpxfft_plan_s &p, AltAxis &a, void *scr, int dir
     const long long w = (long long)a.width, bs = (long long)(a.M * a.width);
     const int M = (int)a.M, conj = dir > 0;
     if (a.fused) {
-        cudaError_t e = run_steps_with<A>(*a.sub, scr, bs, scr, bs, -1, nullptr, 0, a.kernel, M, conj);
-        return e == cudaSuccess ? run_steps_with<A>(*a.sub, scr, bs, scr, bs, +1, nullptr, 0, nullptr, 0, 0) : e;
+        cudaError_t e = run_steps_with<A>(*a.sub, scr, bs, scr, bs, -1, nullptr, 0, a.kernel, M, conj, a.exp_blocks);
+        return e == cudaSuccess
+                   ? run_steps_with<A>(*a.sub, scr, bs, scr, bs, +1, nullptr, 0, nullptr, 0, 0, a.exp_blocks)
+                   : e;
     }
     cudaError_t e = run_columns<A>(*a.sub, scr, -1, scr);
     if (e == cudaSuccess)
@@ -625,10 +643,11 @@ static cudaError_t run_alt_columns(hpxfft_plan_s &p, void *data, int dir)
         // step B's stores, the chirp back in the inverse's step B (which
         // writes only the nx rows of `data`)
         const int L = (int)p.nx, M = (int)a.M;
-        cudaError_t e = run_steps_with<A>(*a.sub, data, dbs, p.alt_buf, sbs, -1, a.chirp, L, a.kernel, M, conj);
-        return e == cudaSuccess
-                   ? run_steps_with<A>(*a.sub, p.alt_buf, sbs, data, dbs, +1, nullptr, 0, a.chirp, L, conj)
-                   : e;
+        cudaError_t e =
+            run_steps_with<A>(*a.sub, data, dbs, p.alt_buf, sbs, -1, a.chirp, L, a.kernel, M, conj, a.exp_blocks);
+        return e == cudaSuccess ? run_steps_with<A>(*a.sub, p.alt_buf, sbs, data, dbs, +1, nullptr, 0, a.chirp, L,
+                                                    conj, a.exp_blocks)
+                                : e;
     }
     cudaError_t e = scale_rows(mode, data, dcy, dbs, p.alt_buf, dcy, sbs, a.chirp, conj, (long long)p.nx,
                                (long long)a.M, dcy, nb, p.stream);
@@ -1063,7 +1082,16 @@ static int alt_tables(hpxfft_plan_s &p, AltAxis &a)
 {
     cudaError_t e = bluestein_tables(a.L, a.M, alt_mode(p.prec), &a.chirp, &a.kernel);
     if (e != cudaSuccess) return cuda_fail(e, "Bluestein tables");
-    a.fused = a.sub->col_two_step && !a.sub->tc_cols && p.prec != HPXFFT_PREC_F64_NATIVE;
+    const hpxfft_plan_s &q = *a.sub;
+    a.fused = q.col_two_step && !q.tc_cols && p.prec != HPXFFT_PREC_F64_NATIVE;
+    // pair exchange between the steps: compiled float-float step shapes
+    if (a.fused && p.prec == HPXFFT_PREC_F64 && q.colA.FL && q.colB.FL && q.colA.L <= kColStepMaxPairL &&
+        q.colB.L <= kColStepMaxPairL) {
+        if (cudaMalloc(&a.exp_blocks, sizeof(int) * q.colA.shape.grid.x * q.batch) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(HPXFFT_ERR_ALLOC, "exponent arrays");
+        }
+    }
     return HPXFFT_OK;
 }
 
@@ -1110,6 +1138,7 @@ static void free_alt(AltAxis &a)
     cudaFree(a.chirp);
     cudaFree(a.kernel);
     cudaFree(a.wtab);
+    cudaFree(a.exp_blocks);
     a = AltAxis{};
 }
 
