@@ -148,7 +148,7 @@ def resource_report(pattern: str | None = None) -> str:
     from collections import defaultdict
 
     nvcc = _nvcc()
-    kernel_sources = [s for s in SOURCES if s.startswith("kernels_") or s == "batch.cu"]
+    kernel_sources = [s for s in SOURCES if s.startswith("kernels_") or s in ("batch.cu", "bluestein.cu")]
     with tempfile.TemporaryDirectory() as tmp:
         cmds = [[nvcc, *ARCH, *NVCC_FLAGS, "-Xptxas", "-v", "-c", os.path.join(CSRC, s), "-o",
                  os.path.join(tmp, s + ".o")] for s in kernel_sources]
