@@ -413,6 +413,10 @@ def run_ours(args):
         kernels["col_kernel"] = stats["second"]
     dominant = max(kernels, key=kernels.get)
     traffic = profiled_traffic(prec, nx, ny, dominant)
+    # DRAM bytes of the whole step from the committed per-kernel ncu traffic
+    # (None unless every kernel of the step was captured)
+    step_traffic = [profiled_traffic(prec, nx, ny, k) for k in kernels]
+    step_dram = sum(step_traffic) if step_traffic and all(t is not None for t in step_traffic) else None
     dom_t = kernels[dominant]
     per_kernel_bytes = B / 2.0
     achieved = per_kernel_bytes / dom_t / 1e9 if dom_t > 0 else 0.0
@@ -475,6 +479,13 @@ def run_ours(args):
                 "traffic_source": "profiles/dram_traffic_%s_%d.md (ncu dram__bytes_read.sum + dram__bytes_write.sum, "
                                   "scaled to a full launch)" % (prec, nx) if traffic else None,
                 "algorithmic_bytes_per_launch": per_kernel_bytes,
+                # the step as a whole: 2 S / t (one read and one write of the
+                # array; a two-pass design reaches at most half the peak on
+                # this count) and the DRAM bytes ncu measured for its kernels
+                "step_2s_gbps": value / 2.0,
+                "step_2s_frac": value / 2.0 / peak,
+                "step_dram_gbps": world * step_dram / (ms * 1e-3) / 1e9 if step_dram else None,
+                "step_dram_frac": world * step_dram / (ms * 1e-3) / 1e9 / peak if step_dram else None,
             },
             "e2e": {
                 "value": world * B / e2e_s / 1e9,
