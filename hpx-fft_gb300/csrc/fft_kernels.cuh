@@ -58,6 +58,12 @@ inline bool factorize_radices(int L, PassPlan &pp)
 // kEPTFixed: elements per thread of the compile-time chains (also their
 // largest radix); they run 1024-thread CTAs.  Runtime-plan kernels keep 16
 // elements per thread and kMaxThreads threads.
+// Compile-time chains run at most 512 threads with a 64-register budget, so
+// two CTAs (and their <= 64 KB of data) share an SM: one streams its strip
+// in or out while the other computes.
+constexpr int kFixedThreadsMax = 512;
+constexpr int kFixedMinBlocks = 2;
+
 struct ArithF32 {
     using T = float;
     using S = float;
@@ -65,6 +71,7 @@ struct ArithF32 {
     static constexpr bool kFixedChains = true;
     static constexpr int kMaxThreads = 1024;
     static constexpr int kEPTFixed = 16;
+    static constexpr int kMinBlocks = kFixedMinBlocks;  // CTAs per SM the compile-time chains keep
 };
 struct ArithF64 {
     using T = double;
@@ -73,6 +80,7 @@ struct ArithF64 {
     static constexpr bool kFixedChains = false;
     static constexpr int kMaxThreads = 512;
     static constexpr int kEPTFixed = 8;
+    static constexpr int kMinBlocks = kFixedMinBlocks;
 };
 struct ArithFF {
     using T = ff;
@@ -81,12 +89,15 @@ struct ArithFF {
     static constexpr bool kFixedChains = true;
     static constexpr int kMaxThreads = 512;
     static constexpr int kEPTFixed = 8;  // 32 data registers within the 64-register budget
+    static constexpr int kMinBlocks = kFixedMinBlocks;
 };
-// Compile-time chains run at most 512 threads with a 64-register budget, so
-// two CTAs (and their <= 64 KB of data) share an SM: one streams its strip
-// in or out while the other computes.
-constexpr int kFixedThreadsMax = 512;
-constexpr int kFixedMinBlocks = 2;
+// Float-float rows of 8192 pairs with radix-16 passes (16 x 16 x 16 x 2):
+// 512 threads at up to 128 registers; the row's 139 KB of shared memory
+// keeps one CTA per SM either way.
+struct ArithFF16 : ArithFF {
+    static constexpr int kEPTFixed = 16;
+    static constexpr int kMinBlocks = 1;
+};
 
 // Elements held per thread in every pass (16 complex values).
 constexpr int kElemsPerThread = 16;
@@ -525,7 +536,7 @@ __device__ __forceinline__ void local_stage(cpx<typename A::T> *s, int L, int lo
 // has at most 512 threads; runtime plans: the type's maximum, one CTA.
 #define HPXFFT_BOUNDS(A, FL)                                                                     \
     __launch_bounds__((FL) > 0 ? fixed_threads(FL, FW, A::kEPTFixed) : A::kMaxThreads,           \
-                      (FL) > 0 && fixed_threads(FL, FW, A::kEPTFixed) <= kFixedThreadsMax ? kFixedMinBlocks : 1)
+                      (FL) > 0 && fixed_threads(FL, FW, A::kEPTFixed) <= kFixedThreadsMax ? A::kMinBlocks : 1)
 
 // ------------------------------------------------------------ row r2c kernel
 // Packed-real row transform: z[m] = x[2m] + i x[2m+1], Z = DFT_M(z), then

@@ -39,6 +39,12 @@ struct RowLaunch {
     static cudaError_t c2r(const RowArgs &a, const LaunchShape &s, int FL, cudaStream_t st);
 };
 
+// The float-float 8192-pair row with radix-16 passes (ArithFF16).
+struct RowLaunchFF16 {
+    static cudaError_t prepare();
+    static cudaError_t r2c(const RowArgs &a, const LaunchShape &s, cudaStream_t st);
+};
+
 template <class A>
 struct ColLaunch {
     static constexpr int kLog2W = sizeof(typename A::S) == 4 ? 3 : 2;  // 64-byte row segments

@@ -110,6 +110,12 @@ struct hpxfft_plan_s {
     // float-float forward column steps with warp-local passes
     // (HPXFFT_FF_WARP_COLS=0 keeps the CTA-wide passes: tests, tuning)
     bool ff_warp_cols = true;
+    // float-float forward rows of 8192 pairs with radix-16 passes
+    // (RowLaunchFF16): their own pass tables and launch shape; the c2r keeps
+    // the radix-8 chain of `row`
+    bool ff_row16 = false;
+    void *row16_ptab = nullptr;
+    hpxfft_gpu::LaunchShape row16_shape{};
     int *exp_rows = nullptr;   // [batch][nx]
     int *exp_step_a = nullptr; // [batch][step A blocks]
     // split-BF16 precision: both column steps (and the rows, for compiled
@@ -389,7 +395,10 @@ static cudaError_t prepare_tc_once()
 static cudaError_t prepare_prec(int prec)
 {
     switch (prec) {
-    case HPXFFT_PREC_F64: return prepare_once<ArithFF>();
+    case HPXFFT_PREC_F64: {
+        cudaError_t e = prepare_once<ArithFF>();
+        return e == cudaSuccess ? RowLaunchFF16::prepare() : e;
+    }
     case HPXFFT_PREC_F64_NATIVE: return prepare_once<ArithF64>();
     case HPXFFT_PREC_BF16X3: {
         cudaError_t e = prepare_once<ArithF32>();
@@ -417,26 +426,35 @@ static cudaError_t gen_pass_twiddles(int prec, void *tab, int Ls, int R, cudaStr
     }
 }
 
-// Allocate and fill the per-pass tables when the dimension uses a fixed chain.
-static int setup_fixed(hpxfft_plan_s &p, DimPlan &d, bool rows, cudaStream_t st, int step = 0)
+// Allocate and fill the per-pass tables of the compile-time chain of length
+// L with radices up to maxR.
+static int chain_tables(hpxfft_plan_s &p, int L, int maxR, void **ptab, cudaStream_t st)
 {
-    d.FL = 0;
-    if (!(step ? has_fixed_step(p.prec, d) : has_fixed(p.prec, rows, d))) return HPXFFT_OK;
-    const auto chain = fixed_chain(d.L, fixed_ept(p.prec));
+    const auto chain = fixed_chain(L, maxR);
     size_t entries = 0;
     for (auto &c : chain)
         if (c.first > 1) entries += (size_t)c.first * (c.second - 1);
-    if (cudaMalloc(&d.ptab, p.tw_elem * (entries ? entries : 1)) != cudaSuccess) {
+    if (cudaMalloc(ptab, p.tw_elem * (entries ? entries : 1)) != cudaSuccess) {
         cudaGetLastError();
         return fail(HPXFFT_ERR_ALLOC, "pass twiddle table");
     }
     size_t off = 0;
     for (auto &c : chain) {
         if (c.first == 1) continue;
-        cudaError_t e = gen_pass_twiddles(p.prec, (char *)d.ptab + off * p.tw_elem, c.first, c.second, st);
+        cudaError_t e = gen_pass_twiddles(p.prec, (char *)*ptab + off * p.tw_elem, c.first, c.second, st);
         if (e != cudaSuccess) return cuda_fail(e, "pass twiddle generation");
         off += (size_t)c.first * (c.second - 1);
     }
+    return HPXFFT_OK;
+}
+
+// Allocate and fill the per-pass tables when the dimension uses a fixed chain.
+static int setup_fixed(hpxfft_plan_s &p, DimPlan &d, bool rows, cudaStream_t st, int step = 0)
+{
+    d.FL = 0;
+    if (!(step ? has_fixed_step(p.prec, d) : has_fixed(p.prec, rows, d))) return HPXFFT_OK;
+    const int rc = chain_tables(p, d.L, fixed_ept(p.prec), &d.ptab, st);
+    if (rc != HPXFFT_OK) return rc;
     d.FL = d.L;
     if (!(step && p.prec == HPXFFT_PREC_BF16X3)) d.shape.threads = fixed_threads(d.L, d.log2W, fixed_ept(p.prec));
     return HPXFFT_OK;
@@ -462,6 +480,13 @@ static RowArgs row_args(const hpxfft_plan_s &p, const void *in, void *out, int a
     a.pairs_out = 0;
     a.exp_out = nullptr;
     a.exp_bstride = (long long)p.nx;
+    return a;
+}
+
+// the forward row arguments with the radix-16 chain's tables
+static RowArgs row16_args(const hpxfft_plan_s &p, RowArgs a)
+{
+    a.ptab = p.row16_ptab;
     return a;
 }
 
@@ -723,6 +748,8 @@ static cudaError_t run_forward(hpxfft_plan_s &p, const void *in, void *out, void
     }
     if (p.alt_row.on)
         e = run_alt_rows<A>(p, in, out);
+    else if (p.ff_row16)
+        e = RowLaunchFF16::r2c(row16_args(p, ra), p.row16_shape, p.stream);
     else if (p.tc_rows)
         e = TcRowLaunch::run(ra, p.tc_dft, p.dev_error, p.row.shape.grid, p.stream);
     else
@@ -818,8 +845,14 @@ static cudaError_t run_forward_pipelined(hpxfft_plan_s &p, void *h)
         }
         LaunchShape rs = p.row.shape;
         rs.grid = dim3((unsigned)(((GA + wrows - 1) / wrows) * p.row.C), (unsigned)p.N2, 1);
-        e = p.tc_rows ? TcRowLaunch::run(ra, p.tc_dft, p.dev_error, rs.grid, p.stream)
-                      : RowLaunch<A>::r2c(ra, rs, p.row.FL, p.stream);
+        if (p.ff_row16) {
+            LaunchShape r16 = p.row16_shape;
+            r16.grid = rs.grid;
+            e = RowLaunchFF16::r2c(row16_args(p, ra), r16, p.stream);
+        } else {
+            e = p.tc_rows ? TcRowLaunch::run(ra, p.tc_dft, p.dev_error, rs.grid, p.stream)
+                          : RowLaunch<A>::r2c(ra, rs, p.row.FL, p.stream);
+        }
         if (e != cudaSuccess) return e;
         ColStepArgs aa = colstep_args(p, 0, d, p.scratch, pairs);
         aa.block_offset = c * GA * stripsA;
@@ -898,7 +931,9 @@ static cudaError_t run_rows_only(hpxfft_plan_s &p, const void *in, void *out)
     if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
     RowArgs ra = row_args(p, in, out, 0);
     ra.prefetch = 1;
-    e = p.alt_row.on ? run_alt_rows<A>(p, in, out) : RowLaunch<A>::r2c(ra, p.row.shape, p.row.FL, p.stream);
+    e = p.alt_row.on  ? run_alt_rows<A>(p, in, out)
+        : p.ff_row16 ? RowLaunchFF16::r2c(row16_args(p, ra), p.row16_shape, p.stream)
+                     : RowLaunch<A>::r2c(ra, p.row.shape, p.row.FL, p.stream);
     if (e != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[2], p.stream)) != cudaSuccess) return e;
@@ -1233,6 +1268,20 @@ static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t
         return fail(HPXFFT_ERR_ALLOC, "twiddle tables");
     }
     int rc = direct_rows ? setup_fixed(*p, p->row, true, p->stream) : HPXFFT_OK;
+    // float-float rows of 8192 pairs: the radix-16 chain (16 x 16 x 16 x 2,
+    // 512 threads at 128 registers) issues fewer instructions than the
+    // radix-8 one (16384^2 rows 2.81 -> 2.72 ms); HPXFFT_FF_ROW16=0 keeps
+    // the radix-8 chain (tests, tuning)
+    if (rc == HPXFFT_OK && direct_rows && precision == HPXFFT_PREC_F64 && p->row.FL == 8192 && p->row.C == 1 &&
+        p->row.log2W == 0) {
+        const char *v = std::getenv("HPXFFT_FF_ROW16");
+        if (!v || strcmp(v, "0") != 0) {
+            rc = chain_tables(*p, 8192, ArithFF16::kEPTFixed, &p->row16_ptab, p->stream);
+            p->row16_shape = p->row.shape;
+            p->row16_shape.threads = fixed_threads(8192, 0, ArithFF16::kEPTFixed);
+            p->ff_row16 = rc == HPXFFT_OK;
+        }
+    }
     if (rc == HPXFFT_OK && direct_cols && !steps_only) rc = setup_fixed(*p, p->col, false, p->stream);
     // column strategy: the two-kernel pass streams 512-byte row segments and
     // wins once the cluster kernel needs 8 or more CTAs per strip (the rule;
@@ -1728,6 +1777,7 @@ int hpxfft_plan_destroy(hpxfft_plan p)
     cudaFree(p->tw_row);
     cudaFree(p->tw_col);
     cudaFree(p->row.ptab);
+    cudaFree(p->row16_ptab);
     cudaFree(p->col.ptab);
     cudaFree(p->colA.ptab);
     cudaFree(p->colB.ptab);

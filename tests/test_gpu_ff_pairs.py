@@ -96,3 +96,22 @@ def test_batch_oop_and_host_path(gpu_lib, cuda, oracle_lib):
         assert np.array_equal(to_complex(pinned), oop)
     for i in range(3):
         assert rel_l2(oop[i], oracle_fwd(oracle_lib, xs[i])) <= 1e-12
+
+
+@pytest.mark.parametrize("row16", ["1", "0"])
+def test_ff_rows_radix16_and_radix8_chains(gpu_lib, cuda, oracle_lib, monkeypatch, row16):
+    """Rows of 8192 float-float pairs run the radix-16 chain by default and
+    the radix-8 one with HPXFFT_FF_ROW16=0: both against the oracle, on the
+    device path and the chunked host path."""
+    monkeypatch.setenv("HPXFFT_FF_ROW16", row16)
+    rng = np.random.default_rng(16)
+    for nx in (24, 8192):  # single-kernel columns; the two-step pass and the pipelined host path
+        x = rng.uniform(-1, 1, (nx, 16384))
+        host = padded(x)
+        ref = oracle_lib.fft_2d_r2c(host.copy(), nthreads=16)
+        with gpu_lib.Plan(nx, host.shape[1], 1, "f64", "estimate") as plan:
+            got = run_device(cuda, plan, host.copy())
+            assert rel_l2(got, ref) <= 1e-12, (row16, nx)
+            pinned = cuda.from_numpy(host.copy()).pin_memory()
+            out = plan.execute_host(pinned.numpy())
+            assert rel_l2(out, ref) <= 1e-12, (row16, nx, "host")
