@@ -493,6 +493,10 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(nx * nc * real_bytes),
                 "d2h_bytes_per_step": int(nx * nc * real_bytes),
                 "ms_per_step": 1e3 * e2e_s,
+                # every timed end-to-end step (the value is their mean; a
+                # step disturbed by the host shows here)
+                "ms_steps": [round(1e3 * t, 3) for t in e2e_times],
+                "ms_median": 1e3 * statistics.median(e2e_times),
                 "h2d_ms": 1e3 * h2d,
                 "d2h_ms": 1e3 * d2h,
                 "host_numa_node": numa_node,
