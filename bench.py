@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the FP32 / batch / backward sections")
     ap.add_argument("--batch-only", action="store_true", help="only the uneven FP32 batch (profiling)")
+    ap.add_argument("--scale-only", action="store_true", help="only the 32768^2 FP64 section (profiling)")
     ap.add_argument("--prime-only", action="store_true",
                     help="only the prime-length transforms beside cuFFT (profiling; --nx/--ny set the size)")
     ap.add_argument("--batch-count", type=int, default=1024)
@@ -667,12 +668,61 @@ def prime_sizes(torch, hpxfft, stream, steps, warm, peak, nx=16381, ny=16382):
     return res
 
 
+def scale_32768(torch, hpxfft, stream, warm, peak, n=32768):
+    """The scale configuration's second size: the FP64 drop-in at 32768^2
+    (8.6 GB in, 8.6 GB out), input uniform[-1,1) plus four integer-frequency
+    sinusoids of amplitude 10 generated on the device (seeded), error
+    against the oracle on the host cores."""
+    import oracle
+
+    nc = 2 * (n // 2 + 1)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(32768)
+    xin = torch.zeros((n, nc), dtype=torch.float64, device="cuda")
+    xin[:, :n] = torch.rand((n, n), generator=g, device="cuda", dtype=torch.float64) * 2 - 1
+    rng = np.random.default_rng(32768)
+    i = torch.arange(n, device="cuda", dtype=torch.float64)[:, None]
+    j = torch.arange(n, device="cuda", dtype=torch.float64)[None, :]
+    for _ in range(4):
+        fx, fy = (int(v) for v in rng.integers(1, n // 2, size=2))
+        for r0 in range(0, n, 4096):  # bounded temporaries
+            xin[r0:r0 + 4096, :n] += 10.0 * torch.sin(2 * math.pi * ((fx * i[r0:r0 + 4096]) % n / n + (fy * j) % n / n))
+    xout = torch.empty_like(xin)
+    B = algorithmic_bytes(n, n, 8)
+    with hpxfft.Plan(n, nc, 1, "f64", "estimate") as p:
+        p.set_stream(stream.cuda_stream)
+        ms = _time_steps(torch, stream, lambda: p.execute_oop(xin.data_ptr(), xout.data_ptr()), 3, warm)
+        p.timing_reset()
+        p.execute_oop(xin.data_ptr(), xout.data_ptr())
+        st = p.timing_stats()
+        p.synchronize()
+    res = {"workload": workload_name(n, n), "ms": ms, "value": B / (ms * 1e-3) / 1e9, "unit": "GB/s",
+           "frac_of_measured_hbm": B / (ms * 1e-3) / 1e9 / peak,
+           "rows_ms": 1e3 * st["first"], "columns_ms": 1e3 * st["second"],
+           "input": "uniform[-1,1) + 4 integer-frequency sinusoids of amplitude 10, generated on the device"}
+    host = xin.cpu().numpy()
+    got = xout.cpu().numpy().view(np.complex128)
+    del xin, xout, i, j
+    torch.cuda.empty_cache()
+    oracle.fft_2d_r2c(host, nthreads=os.cpu_count() or 1)
+    ref = host.view(np.complex128)
+    num = den = mx = 0.0
+    for r0 in range(0, n, 2048):  # chunked: no full-size temporaries
+        d = got[r0:r0 + 2048] - ref[r0:r0 + 2048]
+        num += float(np.vdot(d, d).real)
+        den += float(np.vdot(ref[r0:r0 + 2048], ref[r0:r0 + 2048]).real)
+        mx = max(mx, float(np.abs(d).max()))
+    res["rel_l2_vs_fp64_oracle"], res["max_abs_err_vs_fp64_oracle"] = math.sqrt(num / den), mx
+    return res
+
+
 def extras(torch, hpxfft, args, x64, oracle_ref, peak):
     """The other workloads of this path, measured in the same run:
     FP32 at the same size (precision), 1024 uneven FP32 transforms in one
     persistent graph-replayed launch (batching), the adjoint on 64 FP32
-    2048^2 arrays (differentiation), and a shape with prime lengths
-    (Bluestein's convolution on both passes)."""
+    2048^2 arrays (differentiation), a shape with prime lengths
+    (Bluestein's convolution on both passes), and the FP64 drop-in at 32768^2
+    (the scale configuration's second size)."""
     out = {}
     stream = torch.cuda.current_stream()
     nx, ny = args.nx, args.ny
@@ -728,6 +778,7 @@ def extras(torch, hpxfft, args, x64, oracle_ref, peak):
     del x32, y32
 
     out["prime_sizes"] = prime_sizes(torch, hpxfft, stream, steps, warm, peak)
+    out["scale_32768_f64"] = scale_32768(torch, hpxfft, stream, warm, peak)
 
     # batching: 1024 uneven FP32 instances; "measure": the plan step times
     # queue orders once and caches the winner
@@ -770,6 +821,24 @@ def run_batch_only(args):
     return 0
 
 
+def run_scale_only(args):
+    """The 32768^2 FP64 section alone, one JSON line."""
+    import importlib.util
+
+    import torch
+
+    torch.cuda.set_device(0)
+    spec = importlib.util.spec_from_file_location("hpxfft_build", os.path.join(REPO, "hpx-fft_gb300", "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    b.build_all()
+    import hpxfft
+
+    peak, _ = measured_peak_hbm()
+    print(json.dumps(scale_32768(torch, hpxfft, torch.cuda.current_stream(), max(3, args.warmup), peak)), flush=True)
+    return 0
+
+
 def run_prime_only(args):
     """The prime-length section alone, one JSON line (profiling the
     Bluestein path; --nx/--ny other than the 16384^2 default set the size)."""
@@ -799,6 +868,8 @@ def main():
         return run_batch_only(args)
     if args.prime_only:
         return run_prime_only(args)
+    if args.scale_only:
+        return run_scale_only(args)
     return run_ours(args)
 
 
