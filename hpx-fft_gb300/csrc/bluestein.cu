@@ -11,7 +11,7 @@
 #include <vector>
 
 #include "bluestein.cuh"
-#include "cplx.cuh"
+#include "fft_kernels.cuh"
 
 namespace hpxfft_gpu {
 
@@ -367,6 +367,54 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// blockIdx.x = row * chunks + chunk; thread k of the chunk handles the
+// output pair (k, 2L - k), k = 0..L
+__global__ void __launch_bounds__(256)
+    combine_halves_kernel(const cpx<ff> *y, long long y_bs, const int *y_exp, long long ye_bs, int L,
+                          const cpx<ff> *wz, const cpx<ff> *ws, double *out, long long o_rs, long long o_bs,
+                          int pairs_out, int *exp_out, long long eo_bs, long long nrows, unsigned chunks)
+{
+    const long long r = blockIdx.x / chunks, b = blockIdx.z;
+    const int k = (int)(blockIdx.x % chunks) * 256 + (int)threadIdx.x;
+    const int M = 2 * L;
+    if (r >= nrows || k > L) return;
+    const int e0 = y_exp[b * ye_bs + 2 * r], e1 = y_exp[b * ye_bs + 2 * r + 1];
+    const int E = max(e0, e1);  // kExpNone never wins against a real exponent
+    const float f0 = E == kExpNone || e0 == kExpNone ? 0.0f : pow2_le0(e0 - E);
+    const float f1 = E == kExpNone || e1 == kExpNone ? 0.0f : pow2_le0(e1 - E);
+    const cpx<ff> *y0 = y + b * y_bs + 2 * r * (long long)L, *y1 = y0 + L;
+    const int k1 = k == L ? 0 : k, k2 = (L - k1) % L;  // j mod L for j = k and j = M - k
+    auto ld = [&](const cpx<ff> *p, int i, float f) {
+        const float4 q = __ldcs(reinterpret_cast<const float4 *>(p + i));
+        return cpx<ff>{ff{q.x * f, q.y * f}, ff{q.z * f, q.w * f}};
+    };
+    const cpx<ff> w = wz[k];  // W_M^k; W_M^(M-k) = conj W_M^k
+    const cpx<ff> zk = ld(y0, k1, f0) + cmul(w, ld(y1, k1, f1));
+    const cpx<ff> zp = ld(y0, k2, f0) + cmul(cconj(w), ld(y1, k2, f1));  // Z[M - k]
+    const cpx<ff> zb = cconj(zp);
+    const cpx<ff> e = chalf(zk + zb), o = chalf(zk - zb);
+    const cpx<ff> tk = cmul(ws[k], o);
+    const cpx<ff> xk = e + mul_i<-1>(tk), xm = cconj(e + mul_i<+1>(tk));  // X[k], X[M - k]
+    double *orow = out + b * o_bs + r * o_rs;
+    if (pairs_out) {
+        auto st = [&](long long i, cpx<ff> v) {
+            const ff re = renorm(v.re), im = renorm(v.im);
+            __stcs(reinterpret_cast<float4 *>(orow + 2 * i), make_float4(re.hi, re.lo, im.hi, im.lo));
+        };
+        st(k, xk);
+        if (M - k != k) st(M - k, xm);
+        if (k == 0) exp_out[b * eo_bs + r] = E;
+    } else {
+        const int Eo = E == kExpNone ? 0 : E;
+        auto st = [&](long long i, cpx<ff> v) {
+            __stcs(reinterpret_cast<double2 *>(orow + 2 * i),
+                   make_double2(ff_to_double(renorm(v.re), Eo), ff_to_double(renorm(v.im), Eo)));
+        };
+        st(k, xk);
+        if (M - k != k) st(M - k, xm);
+    }
+}
+
 // ---------------------------------------------------------------- launchers
 
 static long long ceil_div(long long a, long long b) { return (a + b - 1) / b; }
@@ -478,6 +526,21 @@ cudaError_t c2r_merge(int mode, const void *in, long long i_rs, long long i_bs, 
     default: return cudaErrorInvalidValue;
     }
 #undef HPXFFT_M
+    return cudaGetLastError();
+}
+
+cudaError_t combine_halves_split(const void *y, long long y_bs, const int *y_exp, long long ye_bs, int L,
+                                 const void *wz, const void *ws, void *out, long long o_rs, long long o_bs,
+                                 int pairs_out, int *exp_out, long long eo_bs, long long nrows, int batch,
+                                 cudaStream_t st)
+{
+    if (nrows <= 0 || batch <= 0 || L <= 0) return cudaSuccess;
+    const long long chunks = ceil_div(L + 1, 256);
+    if (nrows * chunks > 0x7fffffffLL || batch > 65535) return cudaErrorInvalidValue;
+    const dim3 grid((unsigned)(nrows * chunks), 1, (unsigned)batch);
+    combine_halves_kernel<<<grid, 256, 0, st>>>((const cpx<ff> *)y, y_bs, y_exp, ye_bs, L, (const cpx<ff> *)wz,
+                                               (const cpx<ff> *)ws, (double *)out, o_rs, o_bs, pairs_out, exp_out,
+                                               eo_bs, nrows, (unsigned)chunks);
     return cudaGetLastError();
 }
 

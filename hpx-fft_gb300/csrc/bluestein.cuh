@@ -85,4 +85,15 @@ cudaError_t c2r_merge(int mode, const void *in, long long i_rs, long long i_bs, 
                       const void *chirp, const void *w, int adjoint, void *t, long long t_rs, long long t_bs,
                       long long t_rows, long long t_cols, int batch, cudaStream_t st);
 
+// Rows of 2L float-float pairs from the DFTs of their halves (sub-row c =
+// pairs 2m + c, raw pairs y[b][2r + c][L] with one exponent each in y_exp):
+//   Z[j] = Y0[j mod L] + W_2L^j Y1[j mod L],  j < 2L,
+// then the packed-real split X[k], k = 0..2L, the row kernel's.  Written as
+// raw pairs with one exponent per row (pairs_out, exp_out) or as doubles.
+// wz[k] = W_2L^k and ws[k] = W_4L^k, k = 0..L (float-float tables).
+cudaError_t combine_halves_split(const void *y, long long y_bs, const int *y_exp, long long ye_bs, int L,
+                                 const void *wz, const void *ws, void *out, long long o_rs, long long o_bs,
+                                 int pairs_out, int *exp_out, long long eo_bs, long long nrows, int batch,
+                                 cudaStream_t st);
+
 }  // namespace hpxfft_gpu

@@ -72,6 +72,7 @@ struct ArithF32 {
     static constexpr int kMaxThreads = 1024;
     static constexpr int kEPTFixed = 16;
     static constexpr int kMinBlocks = kFixedMinBlocks;  // CTAs per SM the compile-time chains keep
+    static constexpr int kDecim = 1;  // sub-rows per row (ArithFF16D)
 };
 struct ArithF64 {
     using T = double;
@@ -81,6 +82,7 @@ struct ArithF64 {
     static constexpr int kMaxThreads = 512;
     static constexpr int kEPTFixed = 8;
     static constexpr int kMinBlocks = kFixedMinBlocks;
+    static constexpr int kDecim = 1;  // sub-rows per row (ArithFF16D)
 };
 struct ArithFF {
     using T = ff;
@@ -90,6 +92,7 @@ struct ArithFF {
     static constexpr int kMaxThreads = 512;
     static constexpr int kEPTFixed = 8;  // 32 data registers within the 64-register budget
     static constexpr int kMinBlocks = kFixedMinBlocks;
+    static constexpr int kDecim = 1;  // sub-rows per row (ArithFF16D)
 };
 // Float-float rows of 8192 pairs with radix-16 passes (16 x 16 x 16 x 2):
 // 512 threads at up to 128 registers; the row's 139 KB of shared memory
@@ -97,6 +100,13 @@ struct ArithFF {
 struct ArithFF16 : ArithFF {
     static constexpr int kEPTFixed = 16;
     static constexpr int kMinBlocks = 1;
+};
+// The halves of float-float rows of 16384 pairs, transformed as rows of
+// their own: virtual row v is sub-row c = v % 2 of row v / 2 (its pairs
+// z[2m + c]); its DFT, without the packed-real split, is stored as raw
+// pairs (one exponent per virtual row) for the combining kernel.
+struct ArithFF16D : ArithFF16 {
+    static constexpr int kDecim = 2;
 };
 
 // Elements held per thread in every pass (16 complex values).
@@ -697,8 +707,13 @@ __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bi
 #pragma unroll
             for (int r = 0; r < R1; ++r) {
                 raw[t][r] = V2{};
-                if (active && (NTASK % NT == 0 || task < NTASK) && row < a.nrows)
-                    raw[t][r] = ld_stream(in + row * a.in_stride + 2 * (long long)(jj + r * LR1));
+                if (active && (NTASK % NT == 0 || task < NTASK) && row < a.nrows) {
+                    if constexpr (A::kDecim > 1)  // pair D m + c of row row / D
+                        raw[t][r] = ld_stream(in + (long long)(row / A::kDecim) * a.in_stride +
+                                              2 * ((long long)(jj + r * LR1) * A::kDecim + row % A::kDecim));
+                    else
+                        raw[t][r] = ld_stream(in + row * a.in_stride + 2 * (long long)(jj + r * LR1));
+                }
             }
         }
         if constexpr (A::kScaled) {
@@ -769,7 +784,14 @@ __device__ __forceinline__ void row_r2c_body(const RowArgs &a, int group, int bi
         local_stage<A, -1, C, FL, FW, A::kScaled>(s, L, log2W, a.pp, tw, a.Ltab, ptab, sEc, 2 * (int)crank);
     }
 
-    if constexpr (C == 1) {
+    if constexpr (A::kDecim > 1) {
+        // the sub-row's DFT as raw pairs, its exponent beside it
+        if (row0 < a.nrows) {
+            S *orow = out + (long long)row0 * a.out_stride;
+            for (int k = t0; k < L; k += nth) store_pair<A>(orow + 2 * (long long)k, s[pidx(k)]);
+            if (tid == 0) a.exp_out[(long long)bidx * a.exp_bstride + row0] = block_exp(sEc[0]);
+        }
+    } else if constexpr (C == 1) {
         row_r2c_split<A>(s, a, row0, log2W, tw, out, bidx, sEc, t0, nth);
     } else {
         cg::cluster_group cl = cg::this_cluster();

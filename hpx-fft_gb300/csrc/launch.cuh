@@ -43,6 +43,8 @@ struct RowLaunch {
 struct RowLaunchFF16 {
     static cudaError_t prepare();
     static cudaError_t r2c(const RowArgs &a, const LaunchShape &s, cudaStream_t st);
+    // the two halves of rows of 16384 pairs as rows of their own (ArithFF16D)
+    static cudaError_t halves(const RowArgs &a, const LaunchShape &s, cudaStream_t st);
 };
 
 template <class A>

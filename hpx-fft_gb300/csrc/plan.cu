@@ -116,6 +116,13 @@ struct hpxfft_plan_s {
     bool ff_row16 = false;
     void *row16_ptab = nullptr;
     hpxfft_gpu::LaunchShape row16_shape{};
+    // float-float rows of 16384 pairs as two kernels instead of a two-CTA
+    // cluster: the DFTs of the rows' halves (radix-16 chain, into the column
+    // scratch or half_buf), then the radix-2 combination and the split
+    bool row_halves = false;
+    int *half_exp = nullptr;              // [batch][2 nx] exponents of the half-rows
+    void *half_buf = nullptr;             // when the plan has no column scratch
+    void *half_wz = nullptr, *half_ws = nullptr;  // W_M^k, W_2M^k, k <= M/2
     int *exp_rows = nullptr;   // [batch][nx]
     int *exp_step_a = nullptr; // [batch][step A blocks]
     // split-BF16 precision: both column steps (and the rows, for compiled
@@ -730,6 +737,32 @@ static cudaError_t run_alt_rows_c2r(hpxfft_plan_s &p, void *data, int adjoint)
     return e;
 }
 
+// Float-float rows of 16384 pairs from `in` to `out` in two kernels: the
+// DFTs of their two halves (the column scratch holds them), then the
+// radix-2 combination with the packed-real split (pairs and one exponent
+// per row when pairs_out, else doubles).
+static cudaError_t run_row_halves(hpxfft_plan_s &p, const void *in, void *out, int prefetch_in, int pairs_out,
+                                  int *exp_out)
+{
+    constexpr int L = 8192;
+    void *ybuf = p.scratch ? p.scratch : p.half_buf;
+    RowArgs a = row_args(p, in, ybuf, 0);
+    a.nrows = (int)(2 * p.nx);
+    a.M = L;
+    a.out_stride = 2LL * L;
+    a.out_bstride = 2LL * L * 2 * (long long)p.nx;
+    a.ptab = p.row16_ptab;
+    a.pairs_out = 1;
+    a.exp_out = p.half_exp;
+    a.exp_bstride = 2LL * (long long)p.nx;
+    a.prefetch = prefetch_in;
+    cudaError_t e = RowLaunchFF16::halves(a, p.row16_shape, p.stream);
+    if (e != cudaSuccess) return e;
+    return combine_halves_split(ybuf, 2LL * L * (long long)p.nx, p.half_exp, 2LL * (long long)p.nx, L, p.half_wz,
+                                p.half_ws, out, (long long)p.ncol, (long long)(p.nx * p.ncol), pairs_out, exp_out,
+                                (long long)p.nx, (long long)p.nx, (int)p.batch, p.stream);
+}
+
 // Rows from `in` to `out`, columns on `out`; with the two-step column pass
 // the last step writes `final_out` when it is given (the host buffer of the
 // zero-copy path).
@@ -748,6 +781,8 @@ static cudaError_t run_forward(hpxfft_plan_s &p, const void *in, void *out, void
     }
     if (p.alt_row.on)
         e = run_alt_rows<A>(p, in, out);
+    else if (p.row_halves)
+        e = run_row_halves(p, in, out, prefetch_in, ra.pairs_out, ra.exp_out);
     else if (p.ff_row16)
         e = RowLaunchFF16::r2c(row16_args(p, ra), p.row16_shape, p.stream);
     else if (p.tc_rows)
@@ -792,8 +827,8 @@ static cudaError_t run_inverse(hpxfft_plan_s &p, void *data, int adjoint)
 static bool pipelined_shape(const hpxfft_plan_s &p)
 {
     const int K = hpxfft_plan_s::kChunks;
-    return p.col_two_step && p.batch == 1 && !p.columns_only && !p.rows_only && !p.alt_row.on && p.N1 % K == 0 &&
-           p.N2 % K == 0;
+    return p.col_two_step && p.batch == 1 && !p.columns_only && !p.rows_only && !p.alt_row.on && !p.row_halves &&
+           p.N1 % K == 0 && p.N2 % K == 0;
 }
 
 static cudaError_t ensure_pipeline(hpxfft_plan_s &p)
@@ -931,9 +966,10 @@ static cudaError_t run_rows_only(hpxfft_plan_s &p, const void *in, void *out)
     if ((e = cudaEventRecord(ev[0], p.stream)) != cudaSuccess) return e;
     RowArgs ra = row_args(p, in, out, 0);
     ra.prefetch = 1;
-    e = p.alt_row.on  ? run_alt_rows<A>(p, in, out)
-        : p.ff_row16 ? RowLaunchFF16::r2c(row16_args(p, ra), p.row16_shape, p.stream)
-                     : RowLaunch<A>::r2c(ra, p.row.shape, p.row.FL, p.stream);
+    e = p.alt_row.on    ? run_alt_rows<A>(p, in, out)
+        : p.row_halves ? run_row_halves(p, in, out, 1, 0, nullptr)
+        : p.ff_row16   ? RowLaunchFF16::r2c(row16_args(p, ra), p.row16_shape, p.stream)
+                       : RowLaunch<A>::r2c(ra, p.row.shape, p.row.FL, p.stream);
     if (e != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[1], p.stream)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ev[2], p.stream)) != cudaSuccess) return e;
@@ -1282,6 +1318,29 @@ static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t
             p->ff_row16 = rc == HPXFFT_OK;
         }
     }
+    // float-float rows of 16384 pairs (two-CTA clusters of 8192): the two
+    // kernels of row_halves (32768^2 rows 24.7 -> see design notes);
+    // HPXFFT_FF_ROW_HALVES=0 keeps the cluster kernel
+    if (rc == HPXFFT_OK && direct_rows && precision == HPXFFT_PREC_F64 && p->row.FL == 8192 && p->row.C == 2 &&
+        p->row.log2W == 0) {
+        const char *v = std::getenv("HPXFFT_FF_ROW_HALVES");
+        if (!v || strcmp(v, "0") != 0) {
+            rc = chain_tables(*p, 8192, ArithFF16::kEPTFixed, &p->row16_ptab, p->stream);
+            cudaError_t e2 = cudaSuccess;
+            if (rc == HPXFFT_OK && cudaMalloc(&p->half_exp, sizeof(int) * 2 * p->nx * p->batch) != cudaSuccess) {
+                cudaGetLastError();
+                rc = fail(HPXFFT_ERR_ALLOC, "exponent arrays");
+            }
+            if (rc == HPXFFT_OK && ((e2 = split_table(8192, kTabFF, &p->half_wz)) != cudaSuccess ||
+                                    (e2 = split_table(16384, kTabFF, &p->half_ws)) != cudaSuccess))
+                rc = cuda_fail(e2, "row twiddles");
+            p->row16_shape = p->row.shape;
+            p->row16_shape.threads = fixed_threads(8192, 0, ArithFF16::kEPTFixed);
+            p->row16_shape.cluster = 1;
+            p->row16_shape.grid = dim3((unsigned)(2 * p->nx), (unsigned)p->batch, 1);
+            p->row_halves = rc == HPXFFT_OK;
+        }
+    }
     if (rc == HPXFFT_OK && direct_cols && !steps_only) rc = setup_fixed(*p, p->col, false, p->stream);
     // column strategy: the two-kernel pass streams 512-byte row segments and
     // wins once the cluster kernel needs 8 or more CTAs per strip (the rule;
@@ -1348,6 +1407,11 @@ static int create_plan_with(hpxfft_plan *out, size_t n_row, size_t n_col, size_t
         } else {
             p->ff_pairs = true;
         }
+    }
+    if (rc == HPXFFT_OK && p->row_halves && !p->scratch &&
+        cudaMalloc(&p->half_buf, sizeof(double) * 2 * 16384 * p->nx * p->batch) != cudaSuccess) {
+        cudaGetLastError();
+        rc = fail(HPXFFT_ERR_ALLOC, "row buffer");
     }
     if (rc != HPXFFT_OK) {
         std::string msg = g_last_error;
@@ -1778,6 +1842,10 @@ int hpxfft_plan_destroy(hpxfft_plan p)
     cudaFree(p->tw_col);
     cudaFree(p->row.ptab);
     cudaFree(p->row16_ptab);
+    cudaFree(p->half_exp);
+    cudaFree(p->half_buf);
+    cudaFree(p->half_wz);
+    cudaFree(p->half_ws);
     cudaFree(p->col.ptab);
     cudaFree(p->colA.ptab);
     cudaFree(p->colB.ptab);

@@ -115,3 +115,24 @@ def test_ff_rows_radix16_and_radix8_chains(gpu_lib, cuda, oracle_lib, monkeypatc
             pinned = cuda.from_numpy(host.copy()).pin_memory()
             out = plan.execute_host(pinned.numpy())
             assert rel_l2(out, ref) <= 1e-12, (row16, nx, "host")
+
+
+@pytest.mark.parametrize("halves", ["1", "0"])
+def test_ff_rows_of_16384_pairs_halves_and_cluster(gpu_lib, cuda, oracle_lib, monkeypatch, halves):
+    """Rows of 32768 reals: by default two kernels (the halves' DFTs, then
+    the radix-2 combination with the split), with HPXFFT_FF_ROW_HALVES=0 the
+    two-CTA cluster kernel; against the oracle with the single-kernel column
+    pass (a buffer of their own), the two-step pass (the column scratch, pair
+    exchange) and the host-buffer path."""
+    monkeypatch.setenv("HPXFFT_FF_ROW_HALVES", halves)
+    rng = np.random.default_rng(32)
+    for nx in (24, 4096):
+        x = rng.uniform(-1, 1, (nx, 32768))
+        x[:, ::7] += 3.0
+        host = padded(x)
+        ref = oracle_lib.fft_2d_r2c(host.copy(), nthreads=16)
+        with gpu_lib.Plan(nx, host.shape[1], 1, "f64", "estimate") as plan:
+            got = run_device(cuda, plan, host.copy())
+            assert rel_l2(got, ref) <= 1e-12, (halves, nx)
+            out = plan.execute_host(host.copy())
+            assert rel_l2(out, ref) <= 1e-12, (halves, nx, "host")
