@@ -136,3 +136,25 @@ def test_ff_rows_of_16384_pairs_halves_and_cluster(gpu_lib, cuda, oracle_lib, mo
             assert rel_l2(got, ref) <= 1e-12, (halves, nx)
             out = plan.execute_host(host.copy())
             assert rel_l2(out, ref) <= 1e-12, (halves, nx, "host")
+
+
+def test_ff_rows_of_16384_pairs_batch_and_slab(gpu_lib, cuda, oracle_lib):
+    """The half-row path with a batch of two (per-item strides of the
+    half-row buffer, its exponents and the output) and as the rows-only pass
+    of a two-rank slab decomposition (doubles out, then the slab's own
+    column pass), against the oracle."""
+    rng = np.random.default_rng(3232)
+    nx, ny = 24, 32768
+    xs = rng.uniform(-1, 1, (2, nx, ny))
+    host = np.stack([padded(x) for x in xs])
+    with gpu_lib.Plan(nx, host.shape[-1], 2, "f64", "estimate") as plan:
+        got = run_device(cuda, plan, host.copy())
+    for b in range(2):
+        ref = oracle_lib.fft_2d_r2c(host[b].copy(), nthreads=16)
+        assert rel_l2(got[b], ref) <= 1e-12, b
+    import test_gpu_slab
+
+    x = padded(xs[0])
+    out, _ = test_gpu_slab.run_emulated(gpu_lib, cuda, x, 2, "f64")
+    ref = oracle_lib.fft_2d_r2c(x.copy(), nthreads=16)
+    assert rel_l2(out.view(np.complex128), ref.view(np.complex128)) <= 1e-12
